@@ -1,0 +1,363 @@
+"""Benchmark of the linear-elasticity solve path on GB300.
+
+Workload: 3-D HEXA8 cube 64x64x64 elements on [0,1]^3 (811,200 equations,
+31,442,295 strict-lower CSRC entries), E=1, nu=0.3, z=0 face fixed, unit
+pressure on z=1 as consistent nodal forces, RCM ordering, FP64 Jacobi-PCG to
+1e-8 (the reference's M-norm test).  Synthetic, seeded-free structured mesh.
+
+One step = one pass of the hot path: element integration + CSRC assembly
+(pform_mec isw=2) and the PCG solve to tolerance (solv).  `value` is solves/s
+with the mesh, structure and load vectors already resident on the device;
+`e2e` is the same through the C ABI with host buffers (u, b0 in, b out;
+b in, x out) copied every step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --gpus N > 1 (torchrun, one rank per GPU) every rank solves its own copy
+(the path has no data-parallel exchange: replicas, weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "CSRC-PCG time-to-1e-8 & SpMV HBM GB/s; served solves/s, p99 vs plain FP64"
+WORKLOAD = ("HEXA8 cube 64x64x64 on [0,1]^3, E=1, nu=0.3, z=0 fixed, unit pressure on z=1 "
+            "(nodal forces), RCM, FP64 Jacobi-PCG to 1e-8: assembly + solve per step")
+TOL = 1e-8
+MAXIT = 20000
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, impl):
+        self.ws, self.rank, self.local = _dist()
+        self.pg = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as td
+            backend = "nccl" if (impl == "ours" and torch.cuda.is_available()) else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            td.init_process_group(backend)
+            self.td = td
+            self.backend = backend
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        dev = f"cuda:{self.local}" if self.backend == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{gpu}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [v.strip() for v in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        load = [v for v in sm if v > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per SpMV launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "spmv_fp64_hexa8_cube64.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+def make_workload():
+    from elastic_gb300 import meshgen as M
+    return M.cube_hexa8_64()
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, dist: Dist):
+    import torch
+
+    import elastic_gb300 as E
+
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    mesh = make_workload()
+    ctx = E.Context(device=dev)
+    ctx.set_mesh(mesh)
+    neq, nad, ncolors = ctx.build_structure(True)
+    st = ctx.structure()
+    b0, u0 = E.pload(mesh, st.id)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=dev)
+
+    # ---- device-resident steps
+    ctx.set_state(u0, b0)
+    infos = []
+    for _ in range(args.warmup):
+        ctx.assemble_resident()
+        infos.append(ctx.solve_resident(tol=TOL, maxit=MAXIT))
+    dist.barrier()
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(dev)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev_a = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    launches0 = ctx.kernel_launches
+    ev0.record(ext)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        ev_a[2 * k].record(ext)
+        ctx.assemble_resident()
+        ev_a[2 * k + 1].record(ext)
+        infos.append(ctx.solve_resident(tol=TOL, maxit=MAXIT))
+    ev1.record(ext)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    launches = ctx.kernel_launches - launches0
+    ms_total = ev0.elapsed_time(ev1)
+    asm_ms = statistics.median(ev_a[2 * k].elapsed_time(ev_a[2 * k + 1])
+                               for k in range(args.steps))
+    dist.barrier()
+    ms_total = dist.max(ms_total)
+    ms_step = ms_total / args.steps
+    iters = infos[-1]["iters"]
+
+    # ---- SpMV (the dominant kernel) timed alone on the same stream
+    reps = 50
+    ctx.spmv_resident(reps=5)
+    torch.cuda.synchronize(dev)
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(ext)
+    ctx.spmv_resident(reps=reps)
+    s1.record(ext)
+    torch.cuda.synchronize(dev)
+    clk = clocks.stop()
+    spmv_ms = s0.elapsed_time(s1) / reps
+    spmv_bytes = 12 * nad + 28 * neq
+    spmv_gbs = spmv_bytes / (spmv_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    iter_bytes = 12 * nad + 116 * neq
+    pcg_ms = ms_step - asm_ms
+    iter_gbs = iter_bytes * iters / (pcg_ms * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI with host buffers (pinned)
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    u_h, b0_h = pin(u0), pin(b0)
+    e2e_times = []
+    for k in range(args.warmup + args.steps):
+        dist.barrier()
+        t = time.perf_counter()
+        b_h = ctx.assemble(u_h, b0_h)
+        x_h, info = ctx.solve(b_h, tol=TOL, maxit=MAXIT)
+        dt = time.perf_counter() - t
+        if k >= args.warmup:
+            e2e_times.append(dt)
+    e2e_s = dist.max(sum(e2e_times)) / args.steps
+    h2d = (u0.size + 2 * neq) * 8
+    d2h = 2 * neq * 8
+
+    out = None
+    if dist.rank == 0:
+        n = dist.ws
+        value = n * 1000.0 / ms_step
+        out = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": n,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (structured mesh generated in-process)",
+            "config": {"workload": WORKLOAD, "neq": neq, "nad": nad, "colors": ncolors,
+                       "tol": TOL, "parallelism": "replicas" if n > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (CSRC matrix 400 MB + vectors > 129 MB L2)"},
+            "time_to_tol_ms": ms_step, "pcg_iters": iters, "assembly_ms": asm_ms,
+            "pcg_ms": pcg_ms, "pcg_iter_gbs": iter_gbs, "spmv_ms": spmv_ms,
+            "spmv_gbs": spmv_gbs, "wall_s": wall,
+            "roofline": {"bound": "hbm", "kernel": "pcg_spmv_dot_kernel (FP64 CSRC SpMV)",
+                         "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
+                         "frac": spmv_gbs / peak, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": spmv_bytes,
+                         "traffic": profiled_traffic()},
+            "e2e": {"value": n / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        if n == 1 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(mesh, st, b0, u0, iters, sample_iters=300)
+    ctx.close()
+    return out
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_baseline(mesh, st, b0, u0, full_iters=None, sample_iters=300, nthreads=None):
+    """The reference's OpenMP CPU path (oracle restatement of pform_mec's
+    colour loop and pcg_omp with matvec_csrcsym_omp) on this host's cores:
+    one full assembly plus a bounded PCG sample, extrapolated to the
+    iteration count of the full solve."""
+    import oracle as O
+
+    nth = nthreads or len(os.sched_getaffinity(0))
+    s = O.Structure(perm=st.perm, id=st.id, neq=st.neq, nad=st.nad, ia=st.ia, ja=st.ja)
+    colors = O.colormsh(mesh)
+    t = time.perf_counter()
+    ad, al, b = O.assemble_omp(mesh, s, u0, b0, nthreads=nth, colors=colors)
+    t_asm = time.perf_counter() - t
+    if full_iters is None:
+        _, info = O.pcg_omp(s, ad, al, b, tol=TOL, maxit=MAXIT, nthreads=nth)
+        full_iters = info["iters"]
+        t_pcg = info["seconds"]
+        sample = f"full assembly + full PCG ({full_iters} iterations)"
+    else:
+        n = min(sample_iters, full_iters)
+        _, info = O.pcg_omp(s, ad, al, b, tol=TOL, maxit=n, nthreads=nth, stop_at_maxit=True)
+        t_pcg = info["seconds"] * full_iters / max(info["iters"], 1)
+        sample = (f"full OpenMP assembly + {info['iters']} PCG iterations, scaled to "
+                  f"{full_iters} iterations")
+    total = t_asm + t_pcg
+    return {"value": 1.0 / total, "unit": "solves/s", "cores": nth, "kind": "port",
+            "sample": sample, "seconds_per_solve": total, "assembly_s": t_asm,
+            "pcg_s": t_pcg}
+
+
+def run_reference(args, dist: Dist):
+    """--impl reference: the reference's CPU implementation of the path (the
+    oracle port: OpenMP assembly + pcg_omp) on this host's cores."""
+    if dist.rank != 0:
+        return None
+    import elastic_gb300 as E
+    import oracle as O
+
+    mesh = make_workload()
+    st = E.host_structure(mesh, True)
+    b0, u0 = E.pload(mesh, st.id)
+    s = O.Structure(perm=st.perm, id=st.id, neq=st.neq, nad=st.nad, ia=st.ia, ja=st.ja)
+    nth = len(os.sched_getaffinity(0))
+    colors = O.colormsh(mesh)
+    # the full solve's iteration count, once (needed to scale the samples)
+    ad, al, b = O.assemble_omp(mesh, s, u0, b0, nthreads=nth, colors=colors)
+    _, info = O.pcg_omp(s, ad, al, b, tol=TOL, maxit=MAXIT, nthreads=nth)
+    full_iters = info["iters"]
+    per_step = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(mesh, st, b0, u0, full_iters, sample_iters=150, nthreads=nth)
+        if k >= args.warmup:
+            per_step.append(r["seconds_per_solve"])
+    sec = statistics.median(per_step)
+    value = 1.0 / sec
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": dist.ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec * 1000.0, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (structured mesh)",
+        "config": {"workload": WORKLOAD, "neq": st.neq, "nad": st.nad, "tol": TOL,
+                   "parallelism": f"OpenMP {nth} threads"},
+        "pcg_iters": full_iters,
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nth, "kind": "port",
+                         "sample": ("per step: full OpenMP assembly + 150 pcg_omp iterations "
+                                    f"scaled to the full solve's {full_iters} iterations")},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    dist = Dist(args.impl)
+    try:
+        out = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+    finally:
+        dist.close()
+    if out is not None and dist.rank == 0:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,737 @@
+// C ABI of the library (include/elastic_gb300.h): the context, host<->device
+// staging and the orchestration of the assembly and solver kernels.
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstring>
+
+#include "elx_krylov.h"
+
+using elx::DBuf;
+using elx::Error;
+
+struct elx_ctx {
+  int device = 0;
+  int verbose = 0;
+  cudaStream_t stream = nullptr;
+  int64_t budget = 0, used = 0;
+  std::string err;
+
+  elx::Mesh mesh;
+  elx::Structure s;
+  bool have_mesh = false, have_structure = false, have_matrix = false;
+  bool have_fp32 = false;
+
+  // mesh (colour order) and structure
+  DBuf conn, mat, elnum, slot, x, eq, e;
+  DBuf ia, ja, iat, jat, pt;
+  // matrix
+  DBuf ad, al, alt, ad32, al32, alt32;
+  // state and solver vectors
+  DBuf u, b0, b, xs, r, p, q, m, z;
+  // scalars, partials, counters, flags
+  DBuf scal, partials, counters, flags, diag;
+  elx::PcgScalars *h_scal = nullptr;  // pinned, 2 slots
+  double *h_diag = nullptr;           // pinned
+  int32_t *h_flags = nullptr;         // pinned
+
+  int64_t launches = 0;  // kernels of this library launched by this context
+
+  cudaGraphExec_t pcg_graph = nullptr;
+  int pcg_graph_iters = 0;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+
+  void alloc(DBuf &d, size_t bytes) {
+    release(d);
+    if (bytes == 0) bytes = 16;
+    if (budget > 0 && used + (int64_t)bytes > budget)
+      throw Error{ELX_ERR_OOM, "HBM budget exceeded: need " + std::to_string(bytes) +
+                                   " more bytes, " + std::to_string(budget - used) + " left"};
+    const cudaError_t me = cudaMalloc(&d.p, bytes);
+    if (me != cudaSuccess) {
+      d.p = nullptr;
+      (void)cudaGetLastError();
+      throw Error{ELX_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(me)};
+    }
+    d.bytes = bytes;
+    used += (int64_t)bytes;
+  }
+  void release(DBuf &d) {
+    if (d.p) {
+      cudaFree(d.p);
+      used -= (int64_t)d.bytes;
+    }
+    d.p = nullptr;
+    d.bytes = 0;
+  }
+  template <class T>
+  void upload(DBuf &d, const T *src, size_t n) {
+    alloc(d, n * sizeof(T));
+    if (n) ELX_CUDA(cudaMemcpyAsync(d.p, src, n * sizeof(T), cudaMemcpyHostToDevice, stream));
+  }
+  void sync() { ELX_CUDA(cudaStreamSynchronize(stream)); }
+  void drop_graphs() {
+    if (pcg_graph) cudaGraphExecDestroy(pcg_graph);
+    pcg_graph = nullptr;
+    pcg_graph_iters = 0;
+  }
+
+  elx::MeshDev mesh_dev() const {
+    elx::MeshDev md;
+    md.ndm = mesh.ndm; md.ndf = mesh.ndf; md.nen = mesh.nen; md.numel = mesh.numel;
+    md.nnode = mesh.nnode; md.numat = mesh.numat; md.prop = mesh.prop;
+    md.conn = conn.as<int32_t>(); md.mat = mat.as<int32_t>(); md.elnum = elnum.as<int32_t>();
+    md.slot = slot.as<int32_t>(); md.x = x.as<double>(); md.eq = eq.as<int32_t>();
+    md.e = e.as<double>(); md.npairs = s.npairs;
+    return md;
+  }
+  elx::CsrcDev csrc_dev() const {
+    elx::CsrcDev k;
+    k.neq = s.neq; k.nad = s.nad;
+    k.ia = ia.as<int32_t>(); k.ja = ja.as<int32_t>();
+    k.iat = iat.as<int32_t>(); k.jat = jat.as<int32_t>(); k.pt = pt.as<int32_t>();
+    k.ad = ad.as<double>(); k.al = al.as<double>(); k.alt = alt.as<double>();
+    k.ad32 = ad32.as<float>(); k.al32 = al32.as<float>(); k.alt32 = alt32.as<float>();
+    return k;
+  }
+};
+
+namespace {
+
+template <class F>
+int guarded(elx_ctx *ctx, F &&f) {
+  if (!ctx) return ELX_ERR_ARG;
+  try {
+    ELX_CUDA(cudaSetDevice(ctx->device));
+    f();
+    ctx->err.clear();
+    return ELX_OK;
+  } catch (const Error &e) {
+    ctx->err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    ctx->err = "host allocation failed";
+    return ELX_ERR_OOM;
+  }
+}
+
+void require(bool c, int code, const char *what) {
+  if (!c) throw Error{code, what};
+}
+
+// Uploads everything the kernels need once the structure is known.
+void upload_structure(elx_ctx *c) {
+  const elx::Mesh &m = c->mesh;
+  elx::Structure &s = c->s;
+  c->drop_graphs();
+  elx::derive_structure(m, s);
+  const int nen1 = m.nen + 1;
+  std::vector<int32_t> conn((size_t)m.nen * m.numel), mat(m.numel), elnum(m.numel);
+  for (int t = 0; t < m.numel; t++) {
+    const int el = s.elem_order[t];
+    for (int a = 0; a < m.nen; a++) {
+      int no = m.ix[(size_t)el * nen1 + a];
+      conn[(size_t)a * m.numel + t] = no > 0 ? no - 1 : 0;
+    }
+    mat[t] = m.ix[(size_t)el * nen1 + m.nen] - 1;
+    elnum[t] = el + 1;
+  }
+  std::vector<int32_t> eq(s.id.size());
+  for (size_t q = 0; q < eq.size(); q++) eq[q] = s.id[q] - 1;
+  std::vector<int32_t> ia0(s.ia.size()), ja0(s.ja.size());
+  for (size_t i = 0; i < ia0.size(); i++) ia0[i] = s.ia[i] - 1;
+  for (size_t i = 0; i < ja0.size(); i++) ja0[i] = s.ja[i] - 1;
+  c->upload(c->conn, conn.data(), conn.size());
+  c->upload(c->mat, mat.data(), mat.size());
+  c->upload(c->elnum, elnum.data(), elnum.size());
+  c->upload(c->slot, s.slot.data(), s.slot.size());
+  c->upload(c->x, m.x.data(), m.x.size());
+  c->upload(c->eq, eq.data(), eq.size());
+  c->upload(c->e, m.e.data(), m.e.size());
+  c->upload(c->ia, ia0.data(), ia0.size());
+  c->upload(c->ja, ja0.data(), ja0.size());
+  c->upload(c->iat, s.iat.data(), s.iat.size());
+  c->upload(c->jat, s.jat.data(), s.jat.size());
+  c->upload(c->pt, s.pt.data(), s.pt.size());
+  const size_t n = (size_t)s.neq, nad = (size_t)s.nad;
+  c->alloc(c->ad, n * 8);
+  c->alloc(c->al, nad * 8);
+  c->alloc(c->alt, nad * 8);
+  c->release(c->ad32);
+  c->release(c->al32);
+  c->release(c->alt32);
+  c->have_fp32 = false;
+  c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
+  ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
+  c->alloc(c->b0, n * 8);
+  ELX_CUDA(cudaMemsetAsync(c->b0.p, 0, c->b0.bytes, c->stream));
+  for (DBuf *v : {&c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z}) c->alloc(*v, n * 8);
+  ELX_CUDA(cudaMemsetAsync(c->b.p, 0, c->b.bytes, c->stream));
+  c->alloc(c->scal, sizeof(elx::PcgScalars) * 2);
+  ELX_CUDA(cudaMemsetAsync(c->scal.p, 0, c->scal.bytes, c->stream));  // slot 1: done = 0
+  c->alloc(c->partials, sizeof(double) * 4 * 4096);
+  c->alloc(c->counters, sizeof(unsigned int) * 16);
+  ELX_CUDA(cudaMemsetAsync(c->counters.p, 0, c->counters.bytes, c->stream));
+  c->alloc(c->flags, sizeof(int32_t) * 4);
+  c->alloc(c->diag, sizeof(double) * 8);
+  c->sync();
+  c->have_structure = true;
+  c->have_matrix = false;
+}
+
+[[maybe_unused]] void ensure_fp32(elx_ctx *c) {
+  if (c->have_fp32) return;
+  const size_t n = (size_t)c->s.neq, nad = (size_t)c->s.nad;
+  if (!c->ad32.p) {
+    c->alloc(c->ad32, n * 4);
+    c->alloc(c->al32, nad * 4);
+    c->alloc(c->alt32, nad * 4);
+  }
+  elx::launch_demote_values(c->csrc_dev(), c->stream);
+  c->have_fp32 = true;
+}
+
+void assemble_resident(elx_ctx *c) {
+  require(c->have_structure, ELX_ERR_STATE, "assemble before the structure is set");
+  const elx::Structure &s = c->s;
+  ELX_CUDA(cudaMemsetAsync(c->ad.p, 0, c->ad.bytes, c->stream));
+  ELX_CUDA(cudaMemsetAsync(c->al.p, 0, c->al.bytes, c->stream));
+  ELX_CUDA(cudaMemcpyAsync(c->b.p, c->b0.p, (size_t)s.neq * 8, cudaMemcpyDeviceToDevice,
+                           c->stream));
+  const int32_t big = INT_MAX;
+  int32_t *bad = c->flags.as<int32_t>();
+  ELX_CUDA(cudaMemcpyAsync(bad, &big, sizeof(big), cudaMemcpyHostToDevice, c->stream));
+  const elx::MeshDev md = c->mesh_dev();
+  const elx::CsrcDev k = c->csrc_dev();
+  for (const elx::Segment &seg : s.segments)
+    elx::launch_assembly(md, k, seg, c->u.as<double>(), c->b.as<double>(), bad, c->stream);
+  elx::launch_transpose_values(k, c->stream);
+  c->launches += (int64_t)s.segments.size() + (s.nad ? 1 : 0);
+  ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  c->sync();
+  c->have_fp32 = false;
+  if (c->h_flags[0] != INT_MAX) {
+    c->have_matrix = false;
+    throw Error{ELX_ERR_BAD_DET, "non-positive Jacobian determinant in element " +
+                                     std::to_string(c->h_flags[0])};
+  }
+  c->have_matrix = true;
+}
+
+// Jacobi preconditioner m = 1/ad with the zero-diagonal check of Iters.f:337-342.
+void build_preconditioner(elx_ctx *c) {
+  const int32_t big = INT_MAX;
+  int32_t *zero = c->flags.as<int32_t>() + 1;
+  ELX_CUDA(cudaMemcpyAsync(zero, &big, sizeof(big), cudaMemcpyHostToDevice, c->stream));
+  elx::launch_diag_inverse(c->s.neq, c->ad.as<double>(), c->m.as<double>(), zero, c->stream);
+  c->launches += 1;
+  ELX_CUDA(cudaMemcpyAsync(c->h_flags + 1, zero, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                           c->stream));
+  c->sync();
+  if (c->h_flags[1] != INT_MAX)
+    throw Error{ELX_ERR_ZERO_DIAG, "zero diagonal coefficient in equation " +
+                                       std::to_string(c->h_flags[1])};
+}
+
+constexpr int kBatch = 16;  // PCG iterations per captured graph launch
+
+void capture_pcg_graph(elx_ctx *c) {
+  if (c->pcg_graph && c->pcg_graph_iters == kBatch) return;
+  c->drop_graphs();
+  cudaGraph_t g;
+  ELX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  const elx::CsrcDev k = c->csrc_dev();
+  try {
+    for (int i = 0; i < kBatch; i++)
+      elx::launch_pcg_iteration(k, c->xs.as<double>(), c->r.as<double>(), c->p.as<double>(),
+                                c->q.as<double>(), c->m.as<double>(),
+                                c->scal.as<elx::PcgScalars>(), c->partials.as<double>(),
+                                c->counters.as<unsigned int>(), c->stream);
+  } catch (...) {
+    cudaStreamEndCapture(c->stream, &g);
+    throw;
+  }
+  ELX_CUDA(cudaStreamEndCapture(c->stream, &g));
+  const cudaError_t inst = cudaGraphInstantiate(&c->pcg_graph, g, 0);
+  cudaGraphDestroy(g);
+  ELX_CUDA(inst);
+  c->pcg_graph_iters = kBatch;
+}
+
+void fill_info(elx_ctx *c, elx_info *info, const elx::PcgScalars &sc, double secs) {
+  if (!info) return;
+  const double neq = c->s.neq, nad = (double)c->s.nad;
+  info->iters = sc.iters;
+  info->status = sc.status;
+  info->xkx = c->h_diag[0];
+  info->norm_x = std::sqrt(c->h_diag[1]);
+  info->norm_m_r = std::sqrt(std::fabs(c->h_diag[2]));
+  info->norm_r = std::sqrt(c->h_diag[3]);
+  info->conv = sc.conv;
+  info->seconds = secs;
+  // flop_cg(neq, nad, it, 2) (Matvec.f:1499-1531)
+  const double fl = ((neq + 4.0 * nad) + 2.0 * (2.0 * neq) + 7.0 * neq + 2.0) * sc.iters;
+  info->mflops = secs > 0 ? fl * 1e-6 / secs : 0.0;
+  info->refinements = 0;
+  info->inner_iters = 0;
+}
+
+// y = K x for resident vectors (FP64), with the PCG's own SpMV kernel; the
+// dot product it also forms goes to scalar slot 1 (never marked done).
+void spmv64(elx_ctx *c, const double *x, double *y) {
+  elx::launch_spmv_dot(c->csrc_dev(), x, y, c->scal.as<elx::PcgScalars>() + 1,
+                       c->partials.as<double>(), c->counters.as<unsigned int>() + 4, c->stream);
+  c->launches += 1;
+}
+
+void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  build_preconditioner(c);
+  elx::PcgScalars init{};
+  init.tol = tol;
+  init.maxit = maxit;
+  elx::PcgScalars *d_sc = c->scal.as<elx::PcgScalars>();
+  c->h_scal[0] = init;
+  ELX_CUDA(cudaMemcpyAsync(d_sc, &c->h_scal[0], sizeof(init), cudaMemcpyHostToDevice, c->stream));
+  elx::launch_pcg_start(c->s.neq, c->b.as<double>(), c->m.as<double>(), c->xs.as<double>(),
+                        c->r.as<double>(), c->p.as<double>(), d_sc, c->partials.as<double>(),
+                        c->counters.as<unsigned int>() + 2, c->stream);
+  c->launches += 1;
+  capture_pcg_graph(c);
+  // keep two batches in flight; read the stopping flag of the older one
+  int launched = 0, checked = 0;
+  auto launch_batch = [&](int slot) {
+    ELX_CUDA(cudaGraphLaunch(c->pcg_graph, c->stream));
+    c->launches += 3 * c->pcg_graph_iters;
+    ELX_CUDA(cudaMemcpyAsync(&c->h_scal[slot], d_sc, sizeof(elx::PcgScalars),
+                             cudaMemcpyDeviceToHost, c->stream));
+    ELX_CUDA(cudaEventRecord(c->ev[slot], c->stream));
+  };
+  const int max_batches = maxit / kBatch + 2;
+  launch_batch(0);
+  launched = 1;
+  if (max_batches > 1) {
+    launch_batch(1);
+    launched = 2;
+  }
+  elx::PcgScalars last{};
+  for (;;) {
+    const int slot = checked & 1;
+    ELX_CUDA(cudaEventSynchronize(c->ev[slot]));
+    last = c->h_scal[slot];
+    checked++;
+    if (last.done) break;
+    if (launched >= max_batches) break;  // guard; the kernels stop at maxit themselves
+    launch_batch(launched & 1);
+    launched++;
+  }
+  c->sync();
+  ELX_CUDA(cudaMemcpy(&last, d_sc, sizeof(last), cudaMemcpyDeviceToHost));
+  // post-solve diagnostics (Iters.f:433-458)
+  spmv64(c, c->xs.as<double>(), c->z.as<double>());
+  elx::launch_diagnostics(c->s.neq, c->xs.as<double>(), c->z.as<double>(), c->b.as<double>(),
+                          c->m.as<double>(), c->diag.as<double>(), c->partials.as<double>(),
+                          c->counters.as<unsigned int>() + 3, c->stream);
+  c->launches += 1;
+  ELX_CUDA(cudaMemcpyAsync(c->h_diag, c->diag.p, 4 * sizeof(double), cudaMemcpyDeviceToHost,
+                           c->stream));
+  c->sync();
+  const double secs =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (!last.done) last.status = ELX_ERR_NO_CONVERGENCE;
+  fill_info(c, info, last, secs);
+  if (last.status != ELX_OK)
+    throw Error{last.status, "no convergence after " + std::to_string(last.iters) +
+                                 " iterations"};
+}
+
+void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit, int ngram,
+                    elx_info *info) {
+  require(c->have_matrix, ELX_ERR_STATE, "solve before the matrix is assembled");
+  require(tol > 0 && maxit >= 0, ELX_ERR_ARG, "tol must be > 0 and maxit >= 0");
+  (void)ngram;
+  if (info) std::memset(info, 0, sizeof(*info));
+  if (solver == ELX_SOLVER_PCG && precision == ELX_PREC_FP64) {
+    pcg64(c, tol, maxit, info);
+    return;
+  }
+  throw Error{ELX_ERR_ARG, "solver/precision combination not available"};
+}
+
+void check_mesh(int32_t ndm, int32_t ndf, int32_t nen, int32_t numel, int32_t nnode,
+                const int32_t *ix, const int32_t *ie, int32_t numat, int32_t prop) {
+  require(ndm >= 2 && ndm <= 3 && ndf == ndm && nen >= 3 && nen <= 8 && numel > 0 &&
+              nnode > 0 && numat > 0 && prop >= 3,
+          ELX_ERR_ARG, "invalid mesh sizes");
+  for (int i = 0; i < numat; i++) {
+    const int iel = ie[i];
+    const int nv = elx::elem_nodes(iel);
+    require(nv > 0, ELX_ERR_BAD_ELEMENT, "unsupported element type");
+    require(nv <= nen, ELX_ERR_ARG, "element type needs more nodes than nen");
+    require((iel <= 5) == (ndm == 2), ELX_ERR_ARG, "element type does not match ndm");
+  }
+  const int nen1 = nen + 1;
+  for (int el = 0; el < numel; el++) {
+    const int ma = ix[(size_t)el * nen1 + nen];
+    require(ma >= 1 && ma <= numat, ELX_ERR_ARG, "material number out of range");
+    const int nv = elx::elem_nodes(ie[ma - 1]);
+    for (int a = 0; a < nv; a++) {
+      const int no = ix[(size_t)el * nen1 + a];
+      require(no >= 1 && no <= nnode, ELX_ERR_ARG, "node number out of range");
+    }
+  }
+}
+
+void fill_mesh(elx::Mesh &m, int32_t ndm, int32_t ndf, int32_t nen, int32_t numel,
+               int32_t nnode, const int32_t *ix, const double *x, const int32_t *ie,
+               const double *e, int32_t prop, int32_t numat) {
+  const int nen1 = nen + 1;
+  m.ndm = ndm; m.ndf = ndf; m.nen = nen; m.numel = numel; m.nnode = nnode;
+  m.numat = numat; m.prop = prop;
+  m.ix.assign(ix, ix + (size_t)nen1 * numel);
+  m.x.assign(x, x + (size_t)ndm * nnode);
+  m.ie.assign(ie, ie + numat);
+  m.e.assign(e, e + (size_t)prop * numat);
+}
+
+// graph -> RCM (or natural order) -> numeq -> lower CSRC pattern, on the host.
+void build_host_structure(const elx::Mesh &m, const int32_t *bc, bool reorder,
+                          elx::Structure &s) {
+  std::vector<int32_t> xadj, adj, perm0;
+  elx::node_graph(m, xadj, adj);
+  if (reorder) {
+    elx::rcm_order(m.nnode, xadj, adj, perm0);
+  } else {
+    perm0.resize(m.nnode);
+    for (int i = 0; i < m.nnode; i++) perm0[i] = i;
+  }
+  s.perm.resize(m.nnode);
+  for (int i = 0; i < m.nnode; i++) s.perm[i] = perm0[i] + 1;
+  s.neq = elx::number_equations(m, perm0, bc, s.id);
+  require(s.neq > 0, ELX_ERR_ARG, "no free equations");
+  elx::csrc_pattern(m, s, xadj, adj, s.ia, s.ja);
+  s.nad = (int64_t)s.ia[s.neq] - 1;
+  require(s.nad < INT_MAX, ELX_ERR_ARG, "nad exceeds 32-bit indexing");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *elx_version(void) { return "elastic_gb300 0.1 (sm_103a)"; }
+
+int elx_create(elx_ctx **out, const elx_opts *opts) {
+  if (!out) return ELX_ERR_ARG;
+  *out = nullptr;
+  elx_ctx *c = new (std::nothrow) elx_ctx();
+  if (!c) return ELX_ERR_OOM;
+  if (opts) {
+    c->device = opts->device;
+    c->verbose = opts->verbose;
+    c->budget = opts->hbm_budget;
+  }
+  int st = guarded(c, [&] {
+    int ndev = 0;
+    ELX_CUDA(cudaGetDeviceCount(&ndev));
+    require(c->device >= 0 && c->device < ndev, ELX_ERR_ARG, "no such CUDA device");
+    ELX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    ELX_CUDA(cudaHostAlloc(&c->h_scal, 2 * sizeof(elx::PcgScalars), cudaHostAllocDefault));
+    ELX_CUDA(cudaHostAlloc(&c->h_diag, 8 * sizeof(double), cudaHostAllocDefault));
+    ELX_CUDA(cudaHostAlloc(&c->h_flags, 4 * sizeof(int32_t), cudaHostAllocDefault));
+    for (auto &e : c->ev) ELX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  });
+  if (st != ELX_OK) {
+    // keep the context so that elx_last_error can report why
+    *out = c;
+    return st;
+  }
+  *out = c;
+  return ELX_OK;
+}
+
+void elx_destroy(elx_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->drop_graphs();
+  for (DBuf *d : {&c->conn, &c->mat, &c->elnum, &c->slot, &c->x, &c->eq, &c->e, &c->ia, &c->ja,
+                  &c->iat, &c->jat, &c->pt, &c->ad, &c->al, &c->alt, &c->ad32, &c->al32,
+                  &c->alt32, &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
+                  &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
+    c->release(*d);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->h_scal) cudaFreeHost(c->h_scal);
+  if (c->h_diag) cudaFreeHost(c->h_diag);
+  if (c->h_flags) cudaFreeHost(c->h_flags);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char *elx_last_error(const elx_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+void *elx_stream(elx_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+int64_t elx_device_bytes(const elx_ctx *c) { return c ? c->used : 0; }
+
+int64_t elx_kernel_launches(const elx_ctx *c) { return c ? c->launches : 0; }
+
+int elx_set_mesh(elx_ctx *c, int32_t ndm, int32_t ndf, int32_t nen, int32_t numel,
+                 int32_t nnode, const int32_t *ix, const double *x, const int32_t *ie,
+                 const double *e, int32_t prop, int32_t numat) {
+  return guarded(c, [&] {
+    require(ix && x && ie && e, ELX_ERR_ARG, "null mesh array");
+    check_mesh(ndm, ndf, nen, numel, nnode, ix, ie, numat, prop);
+    fill_mesh(c->mesh, ndm, ndf, nen, numel, nnode, ix, x, ie, e, prop, numat);
+    c->have_mesh = true;
+    c->have_structure = false;
+    c->have_matrix = false;
+  });
+}
+
+int elx_set_structure(elx_ctx *c, int32_t neq, int64_t nad, const int32_t *id,
+                      const int32_t *ia, const int32_t *ja) {
+  return guarded(c, [&] {
+    require(c->have_mesh, ELX_ERR_STATE, "set the mesh first");
+    require(id && ia && (ja || nad == 0) && neq > 0 && nad >= 0 && nad < INT_MAX, ELX_ERR_ARG,
+            "invalid structure arguments");
+    require(ia[0] == 1 && (int64_t)ia[neq] - 1 == nad, ELX_ERR_ARG, "ia inconsistent with nad");
+    const elx::Mesh &m = c->mesh;
+    elx::Structure &s = c->s;
+    s.neq = neq;
+    s.nad = nad;
+    s.id.assign(id, id + (size_t)m.ndf * m.nnode);
+    for (int32_t q : s.id) require(q >= 0 && q <= neq, ELX_ERR_ARG, "id out of range");
+    s.ia.assign(ia, ia + neq + 1);
+    s.ja.assign(ja, ja + nad);
+    for (int i = 0; i < neq; i++) {
+      require(ia[i + 1] >= ia[i], ELX_ERR_ARG, "ia not monotone");
+      for (int32_t k = ia[i]; k < ia[i + 1]; k++) {
+        const int32_t col = ja[k - 1];
+        require(col >= 1 && col <= i, ELX_ERR_ARG, "ja entry not strictly lower");
+        require(k == ia[i] || ja[k - 2] < col, ELX_ERR_ARG, "ja row not ascending");
+      }
+    }
+    s.perm.resize(m.nnode);
+    for (int i = 0; i < m.nnode; i++) s.perm[i] = i + 1;
+    upload_structure(c);
+  });
+}
+
+int elx_build_structure(elx_ctx *c, const int32_t *bc, int32_t reorder) {
+  return guarded(c, [&] {
+    require(c->have_mesh, ELX_ERR_STATE, "set the mesh first");
+    require(bc != nullptr, ELX_ERR_ARG, "null bc");
+    build_host_structure(c->mesh, bc, reorder != 0, c->s);
+    upload_structure(c);
+  });
+}
+
+struct elx_host_structure {
+  elx::Structure s;
+  std::string err;
+};
+
+int elx_host_structure_create(elx_host_structure **out, int32_t ndm, int32_t ndf, int32_t nen,
+                              int32_t numel, int32_t nnode, const int32_t *ix, const int32_t *ie,
+                              int32_t numat, const int32_t *bc, int32_t reorder) {
+  if (!out || !ix || !ie || !bc) return ELX_ERR_ARG;
+  *out = nullptr;
+  try {
+    elx::Mesh m;
+    const std::vector<double> x((size_t)ndm * nnode, 0.0), e((size_t)3 * numat, 0.0);
+    check_mesh(ndm, ndf, nen, numel, nnode, ix, ie, numat, 3);
+    fill_mesh(m, ndm, ndf, nen, numel, nnode, ix, x.data(), ie, e.data(), 3, numat);
+    auto *h = new elx_host_structure();
+    build_host_structure(m, bc, reorder != 0, h->s);
+    *out = h;
+    return ELX_OK;
+  } catch (const Error &e) {
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    return ELX_ERR_OOM;
+  }
+}
+
+int elx_host_structure_sizes(const elx_host_structure *h, int32_t *neq, int64_t *nad) {
+  if (!h) return ELX_ERR_ARG;
+  if (neq) *neq = h->s.neq;
+  if (nad) *nad = h->s.nad;
+  return ELX_OK;
+}
+
+int elx_host_structure_get(const elx_host_structure *h, int32_t *perm, int32_t *id, int32_t *ia,
+                           int32_t *ja) {
+  if (!h) return ELX_ERR_ARG;
+  const elx::Structure &s = h->s;
+  if (perm) std::copy(s.perm.begin(), s.perm.end(), perm);
+  if (id) std::copy(s.id.begin(), s.id.end(), id);
+  if (ia) std::copy(s.ia.begin(), s.ia.end(), ia);
+  if (ja) std::copy(s.ja.begin(), s.ja.end(), ja);
+  return ELX_OK;
+}
+
+void elx_host_structure_destroy(elx_host_structure *h) { delete h; }
+
+int elx_get_sizes(const elx_ctx *c, int32_t *neq, int64_t *nad, int32_t *ncolors) {
+  if (!c) return ELX_ERR_ARG;
+  if (!c->have_structure) return ELX_ERR_STATE;
+  if (neq) *neq = c->s.neq;
+  if (nad) *nad = c->s.nad;
+  if (ncolors) *ncolors = c->s.ncolors;
+  return ELX_OK;
+}
+
+int elx_get_structure(const elx_ctx *c, int32_t *perm, int32_t *id, int32_t *ia, int32_t *ja) {
+  if (!c) return ELX_ERR_ARG;
+  if (!c->have_structure) return ELX_ERR_STATE;
+  const elx::Structure &s = c->s;
+  if (perm) std::copy(s.perm.begin(), s.perm.end(), perm);
+  if (id) std::copy(s.id.begin(), s.id.end(), id);
+  if (ia) std::copy(s.ia.begin(), s.ia.end(), ia);
+  if (ja) std::copy(s.ja.begin(), s.ja.end(), ja);
+  return ELX_OK;
+}
+
+int elx_set_state(elx_ctx *c, const double *u, const double *b0) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "set the structure first");
+    if (u)
+      ELX_CUDA(cudaMemcpyAsync(c->u.p, u, (size_t)c->mesh.ndf * c->mesh.nnode * 8,
+                               cudaMemcpyHostToDevice, c->stream));
+    else
+      ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
+    if (b0)
+      ELX_CUDA(cudaMemcpyAsync(c->b0.p, b0, (size_t)c->s.neq * 8, cudaMemcpyHostToDevice,
+                               c->stream));
+    else
+      ELX_CUDA(cudaMemsetAsync(c->b0.p, 0, c->b0.bytes, c->stream));
+    c->sync();
+  });
+}
+
+int elx_assemble_resident(elx_ctx *c) { return guarded(c, [&] { assemble_resident(c); }); }
+
+int elx_assemble(elx_ctx *c, const double *u, const double *b0, double *b_out, double *ad_out,
+                 double *al_out) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "set the structure first");
+    if (u)
+      ELX_CUDA(cudaMemcpyAsync(c->u.p, u, (size_t)c->mesh.ndf * c->mesh.nnode * 8,
+                               cudaMemcpyHostToDevice, c->stream));
+    else
+      ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
+    if (b0)
+      ELX_CUDA(cudaMemcpyAsync(c->b0.p, b0, (size_t)c->s.neq * 8, cudaMemcpyHostToDevice,
+                               c->stream));
+    else
+      ELX_CUDA(cudaMemsetAsync(c->b0.p, 0, c->b0.bytes, c->stream));
+    assemble_resident(c);
+    const size_t n = (size_t)c->s.neq, nad = (size_t)c->s.nad;
+    if (b_out) ELX_CUDA(cudaMemcpyAsync(b_out, c->b.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (ad_out)
+      ELX_CUDA(cudaMemcpyAsync(ad_out, c->ad.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (al_out && nad)
+      ELX_CUDA(cudaMemcpyAsync(al_out, c->al.p, nad * 8, cudaMemcpyDeviceToHost, c->stream));
+    c->sync();
+  });
+}
+
+int elx_set_matrix(elx_ctx *c, const double *ad, const double *al) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "set the structure first");
+    require(ad && (al || c->s.nad == 0), ELX_ERR_ARG, "null matrix array");
+    ELX_CUDA(cudaMemcpyAsync(c->ad.p, ad, (size_t)c->s.neq * 8, cudaMemcpyHostToDevice,
+                             c->stream));
+    if (c->s.nad)
+      ELX_CUDA(cudaMemcpyAsync(c->al.p, al, (size_t)c->s.nad * 8, cudaMemcpyHostToDevice,
+                               c->stream));
+    elx::launch_transpose_values(c->csrc_dev(), c->stream);
+    c->launches += 1;
+    c->sync();
+    c->have_matrix = true;
+    c->have_fp32 = false;
+  });
+}
+
+int elx_solve_resident(elx_ctx *c, int32_t solver, int32_t precision, double tol,
+                       int32_t maxit, int32_t ngram, elx_info *info) {
+  return guarded(c, [&] { solve_resident(c, solver, precision, tol, maxit, ngram, info); });
+}
+
+int elx_solve(elx_ctx *c, int32_t solver, int32_t precision, double tol, int32_t maxit,
+              int32_t ngram, const double *b, double *x, elx_info *info) {
+  return guarded(c, [&] {
+    require(c->have_matrix, ELX_ERR_STATE, "solve before the matrix is assembled");
+    require(b && x, ELX_ERR_ARG, "null b or x");
+    ELX_CUDA(cudaMemcpyAsync(c->b.p, b, (size_t)c->s.neq * 8, cudaMemcpyHostToDevice,
+                             c->stream));
+    int st = ELX_OK;
+    try {
+      solve_resident(c, solver, precision, tol, maxit, ngram, info);
+    } catch (const Error &e) {
+      if (e.code != ELX_ERR_NO_CONVERGENCE) throw;
+      st = e.code;
+      c->err = e.msg;
+    }
+    ELX_CUDA(cudaMemcpyAsync(x, c->xs.p, (size_t)c->s.neq * 8, cudaMemcpyDeviceToHost,
+                             c->stream));
+    c->sync();
+    if (st != ELX_OK) throw Error{st, c->err};
+  });
+}
+
+int elx_update(elx_ctx *c, const double *x, double *u) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "set the structure first");
+    require(x && u, ELX_ERR_ARG, "null x or u");
+    const std::vector<int32_t> &id = c->s.id;
+    for (size_t q = 0; q < id.size(); q++)
+      if (id[q] > 0) u[q] = x[id[q] - 1];
+  });
+}
+
+int elx_spmv(elx_ctx *c, int32_t precision, const double *x, double *y) {
+  return guarded(c, [&] {
+    require(c->have_matrix, ELX_ERR_STATE, "no matrix");
+    require(x && y, ELX_ERR_ARG, "null x or y");
+    const size_t n = (size_t)c->s.neq;
+    ELX_CUDA(cudaMemcpyAsync(c->p.p, x, n * 8, cudaMemcpyHostToDevice, c->stream));
+    if (precision == ELX_PREC_FP64) {
+      spmv64(c, c->p.as<double>(), c->q.as<double>());
+    } else {
+      throw Error{ELX_ERR_ARG, "precision not available"};
+    }
+    ELX_CUDA(cudaMemcpyAsync(y, c->q.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    c->sync();
+  });
+}
+
+int elx_spmv_resident(elx_ctx *c, int32_t precision, int32_t reps) {
+  return guarded(c, [&] {
+    require(c->have_matrix, ELX_ERR_STATE, "no matrix");
+    require(precision == ELX_PREC_FP64, ELX_ERR_ARG, "precision not available");
+    for (int i = 0; i < reps; i++) spmv64(c, c->p.as<double>(), c->q.as<double>());
+  });
+}
+
+int elx_get_solution(elx_ctx *c, double *x) {
+  return guarded(c, [&] {
+    require(c->have_structure && x, ELX_ERR_ARG, "no structure or null x");
+    ELX_CUDA(cudaMemcpyAsync(x, c->xs.p, (size_t)c->s.neq * 8, cudaMemcpyDeviceToHost,
+                             c->stream));
+    c->sync();
+  });
+}
+
+int elx_get_rhs(elx_ctx *c, double *b) {
+  return guarded(c, [&] {
+    require(c->have_structure && b, ELX_ERR_ARG, "no structure or null b");
+    ELX_CUDA(cudaMemcpyAsync(b, c->b.p, (size_t)c->s.neq * 8, cudaMemcpyDeviceToHost,
+                             c->stream));
+    c->sync();
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,133 @@
+// Internal declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "elastic_gb300.h"
+
+namespace elx {
+
+// ---------------------------------------------------------------- errors
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define ELX_CUDA(call)                                                      \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess)                                                  \
+      throw ::elx::Error{ELX_ERR_CUDA, std::string(#call) + ": " +          \
+                                           cudaGetErrorString(e_)};         \
+  } while (0)
+
+#define ELX_REQUIRE(cond, code, what)                                       \
+  do {                                                                      \
+    if (!(cond)) throw ::elx::Error{(code), (what)};                        \
+  } while (0)
+
+// ------------------------------------------------------- device buffers
+// Owning device allocation; every allocation of a context goes through
+// Ctx::alloc so that the HBM budget is enforced in one place.
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  template <class T>
+  T *as() const { return static_cast<T *>(p); }
+};
+
+// ------------------------------------------------------ host structure
+// Element type codes of the reference (Elmlib.f:43-144).
+enum ElemType : int32_t {
+  TRIA3_STRAIN = 2,
+  TRIA3_STRESS = 3,
+  QUAD4_STRAIN = 4,
+  QUAD4_STRESS = 5,
+  TETRA4 = 6,
+  HEXA8 = 7
+};
+int elem_nodes(int iel);  // vertex count, 0 if unsupported
+
+struct Mesh {
+  int32_t ndm = 0, ndf = 0, nen = 0, numel = 0, nnode = 0, numat = 0, prop = 0;
+  std::vector<int32_t> ix;  // (nen+1, numel), 1-based contents
+  std::vector<double> x;    // (ndm, nnode)
+  std::vector<int32_t> ie;  // (numat)
+  std::vector<double> e;    // (prop, numat)
+};
+
+// One launch segment of the assembly: elements [begin, end) of the colour-
+// ordered element list, all of the same element type.
+struct Segment {
+  int32_t iel, begin, end;
+};
+
+struct Structure {
+  int32_t neq = 0;
+  int64_t nad = 0;
+  std::vector<int32_t> perm;  // (nnode) 1-based, RCM order (identity if given)
+  std::vector<int32_t> id;    // (ndf, nnode) 1-based equation numbers, 0 = fixed
+  std::vector<int32_t> ia;    // (neq+1) 1-based
+  std::vector<int32_t> ja;    // (nad)   1-based
+  // derived, 0-based
+  std::vector<int32_t> iat, jat, pt;    // transposed index: CSR of the upper part
+  std::vector<int32_t> elem_order;      // colour-ordered element list (0-based)
+  std::vector<Segment> segments;        // per colour and element type
+  std::vector<int32_t> color_of_segment;
+  int32_t ncolors = 0;
+  std::vector<int32_t> slot;            // (npairs, numel) in colour order
+  int32_t npairs = 0;
+};
+
+// host structure routines (structure.cpp)
+void node_graph(const Mesh &m, std::vector<int32_t> &xadj, std::vector<int32_t> &adj);
+void rcm_order(int32_t n, const std::vector<int32_t> &xadj,
+               const std::vector<int32_t> &adj, std::vector<int32_t> &perm);
+int32_t number_equations(const Mesh &m, const std::vector<int32_t> &perm,
+                         const int32_t *bc, std::vector<int32_t> &id);
+void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> &xadj,
+                  const std::vector<int32_t> &adj, std::vector<int32_t> &ia,
+                  std::vector<int32_t> &ja);
+void derive_structure(const Mesh &m, Structure &s);
+
+// ------------------------------------------------------------- kernels
+struct MeshDev {
+  int32_t ndm, ndf, nen, numel, nnode, numat, prop;
+  const int32_t *conn;   // (nen, numel) 0-based node, colour order, SoA
+  const int32_t *mat;    // (numel) 0-based material, colour order
+  const int32_t *elnum;  // (numel) original 1-based element number
+  const int32_t *slot;   // (npairs, numel) colour order
+  const double *x;       // (ndm, nnode)
+  const int32_t *eq;     // (ndf, nnode) 0-based equation or -1
+  const double *e;       // (prop, numat)
+  int32_t npairs;
+};
+
+struct CsrcDev {
+  int32_t neq;
+  int64_t nad;
+  const int32_t *ia;   // (neq+1) 0-based positions
+  const int32_t *ja;   // (nad)   0-based columns
+  const int32_t *iat;  // (neq+1) upper part row pointers
+  const int32_t *jat;  // (nad)   upper part columns (= lower-part row)
+  const int32_t *pt;   // (nad)   position in al of each upper entry
+  double *ad, *al, *alt;
+  float *ad32, *al32, *alt32;
+};
+
+// assemble.cu
+void launch_assembly(const MeshDev &m, const CsrcDev &k, const Segment &seg,
+                     const double *u, double *b, int32_t *bad_elem,
+                     cudaStream_t st);
+// spmv.cu
+void launch_spmv64(const CsrcDev &k, const double *x, double *y, cudaStream_t st);
+void launch_spmv32(const CsrcDev &k, const float *x, float *y, cudaStream_t st);
+void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
+void launch_demote_values(const CsrcDev &k, cudaStream_t st);
+
+}  // namespace elx

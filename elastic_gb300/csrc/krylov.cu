@@ -1,0 +1,277 @@
+// Jacobi-preconditioned CG on the GPU (pcg, mef/src/Iters.f:252-524, with
+// the diagonal preconditioner of Solv.f:65-69 / Precond.f:22-45).
+//
+// One iteration is three kernels that keep every scalar on the device, so the
+// host never waits inside the loop:
+//   1. q = K p fused with the dot (p, q); the last block to finish computes
+//      alpha = d / (p, q)                                   (Iters.f:366-372)
+//   2. x += alpha p, r -= alpha q, z = M r (not stored) fused with (r, z);
+//      the last block computes beta, d and the stopping test
+//      sqrt|d| < tol * ||b||_M                              (Iters.f:377-419)
+//   3. p = M r + beta p                                     (Iters.f:411-414)
+// Every kernel returns at once when the stopping flag is set, so the host can
+// enqueue iterations in batches (captured once as a CUDA graph) and read the
+// flag between batches.  Reductions are two-level with a fixed grid: each
+// block reduces its threads in a fixed tree and the last block to arrive
+// sums the block partials in a fixed order, so results are deterministic.
+#include "elx_krylov.h"
+
+namespace elx {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kLanes = 8;                       // threads per SpMV row
+constexpr int kRowsPerBlock = kThreads / kLanes;
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// Block-wide sum of NV values (fixed order); result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+  __shared__ double sh[NV][kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    v[i] = warp_sum(v[i]);
+    if (lane == 0) sh[i][w] = v[i];
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      double t = lane < kThreads / 32 ? sh[i][lane] : 0.0;
+      v[i] = warp_sum(t);
+    }
+  }
+}
+
+// Writes this block's NV partials and returns true in thread 0 of the last
+// block to arrive, after which that thread may read every block's partials.
+template <int NV>
+__device__ __forceinline__ bool publish_partials(const double (&v)[NV], double *partials,
+                                                 unsigned int *counter) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; i++) partials[(size_t)i * gridDim.x + blockIdx.x] = v[i];
+    __threadfence();
+    const unsigned int ticket = atomicAdd(counter, 1u);
+    last = ticket == gridDim.x - 1;
+  }
+  __syncthreads();
+  return last;
+}
+
+// In the last block: every thread sums a strided slice of the partials, then
+// a fixed tree; thread 0 gets the totals and resets the counter.
+template <int NV>
+__device__ __forceinline__ void gather_partials(double (&tot)[NV], const double *partials,
+                                                unsigned int *counter) {
+  __threadfence();
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads)
+      s += ((volatile const double *)partials)[(size_t)i * gridDim.x + b];
+    tot[i] = s;
+  }
+  block_sum<NV>(tot);
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// ------------------------------------------------------------ kernels
+__global__ void __launch_bounds__(kThreads)
+diag_inverse_kernel(int n, const double *__restrict__ ad, double *__restrict__ m,
+                    int32_t *zero_row) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double a = ad[i];
+    if (a == 0.0) atomicMin(zero_row, i + 1);
+    m[i] = 1.0 / a;
+  }
+}
+
+// x = 0, r = b, p = M b and d = (b, M b); conv = tol * sqrt|d| (Iters.f:343-360
+// with x0 = 0, for which K x0 = 0 and r0 = b exactly).
+__global__ void __launch_bounds__(kThreads)
+pcg_start_kernel(int n, const double *__restrict__ b, const double *__restrict__ m,
+                 double *__restrict__ x, double *__restrict__ r, double *__restrict__ p,
+                 PcgScalars *sc, double *partials, unsigned int *counter) {
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double bi = b[i], zi = bi * m[i];
+    x[i] = 0.0;
+    r[i] = bi;
+    p[i] = zi;
+    v[0] += bi * zi;
+  }
+  block_sum<1>(v);
+  if (!publish_partials<1>(v, partials, counter)) return;
+  double tot[1];
+  gather_partials<1>(tot, partials, counter);
+  if (threadIdx.x == 0) {
+    sc->d = tot[0];
+    sc->bmb = tot[0];
+    sc->conv = sc->tol * sqrt(fabs(tot[0]));
+    sc->iters = 0;
+    sc->status = 0;
+    // b = 0: x = 0 is exact; the reference would divide 0 by 0 here.
+    sc->done = (tot[0] == 0.0 || sc->maxit <= 0) ? 1 : 0;
+    if (sc->maxit <= 0 && tot[0] != 0.0) sc->status = ELX_ERR_NO_CONVERGENCE;
+  }
+}
+
+// q = K p and (p, q); alpha = d / (p, q).
+__global__ void __launch_bounds__(kThreads)
+pcg_spmv_dot_kernel(CsrcDev k, const double *__restrict__ p, double *__restrict__ q,
+                    PcgScalars *sc, double *partials, unsigned int *counter) {
+  if (sc->done) return;
+  const int lane = threadIdx.x % kLanes, sub = threadIdx.x / kLanes;
+  double v[1] = {0.0};
+  for (int row0 = blockIdx.x * kRowsPerBlock; row0 < k.neq; row0 += gridDim.x * kRowsPerBlock) {
+    const int row = row0 + sub;
+    double s = 0.0;
+    if (row < k.neq) {
+      for (int j = k.ia[row] + lane; j < k.ia[row + 1]; j += kLanes) s += k.al[j] * p[k.ja[j]];
+      for (int j = k.iat[row] + lane; j < k.iat[row + 1]; j += kLanes) s += k.alt[j] * p[k.jat[j]];
+    }
+#pragma unroll
+    for (int off = kLanes / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, kLanes);
+    if (row < k.neq && lane == 0) {
+      const double pi = p[row];
+      const double qi = k.ad[row] * pi + s;
+      q[row] = qi;
+      v[0] += pi * qi;
+    }
+  }
+  block_sum<1>(v);
+  if (!publish_partials<1>(v, partials, counter)) return;
+  double tot[1];
+  gather_partials<1>(tot, partials, counter);
+  if (threadIdx.x == 0) {
+    sc->pq = tot[0];
+    sc->alpha = sc->d / tot[0];
+  }
+}
+
+// x += alpha p; r -= alpha q; (r, M r); beta, d, stopping test.
+__global__ void __launch_bounds__(kThreads)
+pcg_update_kernel(int n, const double *__restrict__ p, const double *__restrict__ q,
+                  const double *__restrict__ m, double *__restrict__ x,
+                  double *__restrict__ r, PcgScalars *sc, double *partials,
+                  unsigned int *counter) {
+  if (sc->done) return;
+  const double alpha = sc->alpha;
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    x[i] += alpha * p[i];
+    const double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    v[0] += ri * (ri * m[i]);
+  }
+  block_sum<1>(v);
+  if (!publish_partials<1>(v, partials, counter)) return;
+  double tot[1];
+  gather_partials<1>(tot, partials, counter);
+  if (threadIdx.x == 0) {
+    const double di = tot[0];
+    sc->beta = di / sc->d;
+    sc->d = di;
+    const int it = sc->iters + 1;
+    sc->iters = it;
+    if (sqrt(fabs(di)) < sc->conv) {
+      sc->done = 1;
+    } else if (it >= sc->maxit || !(di == di)) {
+      sc->done = 1;
+      sc->status = ELX_ERR_NO_CONVERGENCE;
+    }
+  }
+}
+
+// p = M r + beta p.
+__global__ void __launch_bounds__(kThreads)
+pcg_direction_kernel(int n, const double *__restrict__ r, const double *__restrict__ m,
+                     double *__restrict__ p, const PcgScalars *sc) {
+  if (sc->done) return;
+  const double beta = sc->beta;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+    p[i] = r[i] * m[i] + beta * p[i];
+}
+
+// Post-solve diagnostics (Iters.f:433-458): z = K x is given; r = b - z;
+// xKx = (x, z), ||x||^2, (r, M r), (r, r).
+__global__ void __launch_bounds__(kThreads)
+diagnostics_kernel(int n, const double *__restrict__ x, const double *__restrict__ z,
+                   const double *__restrict__ b, const double *__restrict__ m,
+                   double *out, double *partials, unsigned int *counter) {
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double xi = x[i], zi = z[i], ri = b[i] - zi;
+    v[0] += xi * zi;
+    v[1] += xi * xi;
+    v[2] += ri * (ri * m[i]);
+    v[3] += ri * ri;
+  }
+  block_sum<4>(v);
+  if (!publish_partials<4>(v, partials, counter)) return;
+  double tot[4];
+  gather_partials<4>(tot, partials, counter);
+  if (threadIdx.x == 0)
+    for (int i = 0; i < 4; i++) out[i] = tot[i];
+}
+
+}  // namespace
+
+int vector_grid(int n) {
+  // a fixed multiple of the SM count keeps the partial count small and fixed
+  int g = (n + kThreads - 1) / kThreads;
+  return g < 1216 ? (g < 1 ? 1 : g) : 1216;
+}
+
+int spmv_grid(int neq) {
+  int g = (neq + kRowsPerBlock - 1) / kRowsPerBlock;
+  return g < 2432 ? (g < 1 ? 1 : g) : 2432;
+}
+
+void launch_diag_inverse(int n, const double *ad, double *m, int32_t *zero_row, cudaStream_t st) {
+  diag_inverse_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, ad, m, zero_row);
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_pcg_start(int n, const double *b, const double *m, double *x, double *r, double *p,
+                      PcgScalars *sc, double *partials, unsigned int *counter, cudaStream_t st) {
+  pcg_start_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, b, m, x, r, p, sc, partials, counter);
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_pcg_iteration(const CsrcDev &k, double *x, double *r, double *p, double *q,
+                          const double *m, PcgScalars *sc, double *partials,
+                          unsigned int *counters, cudaStream_t st) {
+  const int n = k.neq;
+  pcg_spmv_dot_kernel<<<spmv_grid(n), kThreads, 0, st>>>(k, p, q, sc, partials, counters + 0);
+  pcg_update_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, p, q, m, x, r, sc, partials,
+                                                         counters + 1);
+  pcg_direction_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, r, m, p, sc);
+  ELX_CUDA(cudaGetLastError());
+}
+
+// The PCG's fused SpMV as a standalone product y = K x (the dot it also
+// forms lands in the scalars at sc, which must have done == 0).
+void launch_spmv_dot(const CsrcDev &k, const double *x, double *y, PcgScalars *sc,
+                     double *partials, unsigned int *counter, cudaStream_t st) {
+  pcg_spmv_dot_kernel<<<spmv_grid(k.neq), kThreads, 0, st>>>(k, x, y, sc, partials, counter);
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_diagnostics(int n, const double *x, const double *z, const double *b,
+                        const double *m, double *out, double *partials, unsigned int *counter,
+                        cudaStream_t st) {
+  diagnostics_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, x, z, b, m, out, partials, counter);
+  ELX_CUDA(cudaGetLastError());
+}
+
+}  // namespace elx

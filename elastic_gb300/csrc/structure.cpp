@@ -1,0 +1,374 @@
+// Host-side structure of the solve path: node graph, RCM permutation,
+// equation numbering and the lower CSRC pattern (all bit-identical to the
+// reference's), plus what the GPU kernels need beyond the reference's
+// arrays: the transposed index of the strict lower part, an element colouring
+// and the per-element slot map used by the assembly kernels.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+
+#include "elx_internal.h"
+
+namespace elx {
+
+int elem_nodes(int iel) {
+  switch (iel) {
+    case TRIA3_STRAIN:
+    case TRIA3_STRESS: return 3;
+    case QUAD4_STRAIN:
+    case QUAD4_STRESS:
+    case TETRA4: return 4;
+    case HEXA8: return 8;
+    default: return 0;
+  }
+}
+
+// Node adjacency: for every node the ascending list of distinct other nodes
+// that share an element with it.  Same lists as graph/aponta/graph0/graph1
+// (mef/src/Graph.f:20-208); node numbers 0 or > nnode are skipped as there.
+// Output is 0-based: neighbours of node v are adj[xadj[v] .. xadj[v+1]).
+void node_graph(const Mesh &m, std::vector<int32_t> &xadj, std::vector<int32_t> &adj) {
+  const int nen1 = m.nen + 1;
+  std::vector<int32_t> cnt(m.nnode + 1, 0);
+  for (int el = 0; el < m.numel; el++)
+    for (int a = 0; a < m.nen; a++) {
+      int no = m.ix[(size_t)el * nen1 + a];
+      if (no <= 0 || no > m.nnode) continue;
+      cnt[no] += m.nen - 1;
+    }
+  std::vector<int64_t> start(m.nnode + 1, 0);
+  for (int v = 0; v < m.nnode; v++) start[v + 1] = start[v] + cnt[v + 1];
+  std::vector<int32_t> raw(start[m.nnode]);
+  std::vector<int64_t> fill(start.begin(), start.end() - 1);
+  for (int el = 0; el < m.numel; el++) {
+    const int32_t *c = &m.ix[(size_t)el * nen1];
+    for (int a = 0; a < m.nen; a++) {
+      int na = c[a];
+      if (na <= 0 || na > m.nnode) continue;
+      for (int b = 0; b < m.nen; b++) {
+        int nb = c[b];
+        if (nb <= 0 || nb > m.nnode || nb == na) continue;
+        raw[fill[na - 1]++] = nb - 1;
+      }
+    }
+  }
+  xadj.assign(m.nnode + 1, 0);
+  adj.clear();
+  adj.reserve(raw.size() / 2 + 1);
+  for (int v = 0; v < m.nnode; v++) {
+    auto b = raw.begin() + start[v], e = raw.begin() + fill[v];
+    std::sort(b, e);
+    auto last = std::unique(b, e);
+    adj.insert(adj.end(), b, last);
+    xadj[v + 1] = (int32_t)adj.size();
+  }
+}
+
+namespace {
+
+// Breadth-first level structure of the masked component containing root
+// (rootls, Reord.f:278-354).  Returns the number of levels; ls holds the
+// nodes level by level, xls[l] the start of level l (xls[nlvl] = size).
+int level_structure(int root, const std::vector<int32_t> &xadj,
+                    const std::vector<int32_t> &adj, std::vector<char> &mask,
+                    int32_t *ls, std::vector<int32_t> &xls) {
+  mask[root] = 0;
+  ls[0] = root;
+  int nlvl = 0, lvl_end = 0, size = 1;
+  for (;;) {
+    int lvl_begin = lvl_end;
+    lvl_end = size;
+    xls[nlvl++] = lvl_begin;
+    for (int i = lvl_begin; i < lvl_end; i++) {
+      int v = ls[i];
+      for (int k = xadj[v]; k < xadj[v + 1]; k++) {
+        int w = adj[k];
+        if (!mask[w]) continue;
+        mask[w] = 0;
+        ls[size++] = w;
+      }
+    }
+    if (size == lvl_end) break;
+  }
+  xls[nlvl] = lvl_end;
+  for (int i = 0; i < size; i++) mask[ls[i]] = 1;
+  return nlvl;
+}
+
+// Pseudo-peripheral node of the masked component of root: the
+// Gibbs-Poole-Stockmeyer variant of fnroot (Reord.f:101-169).  Among the
+// nodes of the last level it picks the first one of strictly smallest masked
+// degree, and repeats while the level count grows.
+int pseudo_peripheral(int root, const std::vector<int32_t> &xadj,
+                      const std::vector<int32_t> &adj, std::vector<char> &mask,
+                      int32_t *ls, std::vector<int32_t> &xls) {
+  int nlvl = level_structure(root, xadj, adj, mask, ls, xls);
+  int size = xls[nlvl];
+  if (nlvl == 1 || nlvl == size) return root;
+  for (;;) {
+    int first = xls[nlvl - 1];
+    int mindeg = size;
+    root = ls[first];
+    if (size - 1 != first) {
+      for (int j = first; j < size; j++) {
+        int v = ls[j], deg = 0;
+        for (int k = xadj[v]; k < xadj[v + 1]; k++) deg += mask[adj[k]] ? 1 : 0;
+        if (deg < mindeg) {
+          root = v;
+          mindeg = deg;
+        }
+      }
+    }
+    int nl = level_structure(root, xadj, adj, mask, ls, xls);
+    if (nl <= nlvl) return root;
+    nlvl = nl;
+    if (nlvl >= size) return root;
+  }
+}
+
+}  // namespace
+
+// Reverse Cuthill-McKee ordering of every connected component, components in
+// the order of their lowest-numbered node, as genrcm/rcm/degree do
+// (Reord.f:45-100, 170-277, 355-435): breadth first from a pseudo-peripheral
+// root, the unnumbered neighbours of each node appended in adjacency order and
+// then stably sorted by increasing masked degree, the component reversed at
+// the end.  perm[k] = 0-based old node at new position k.
+void rcm_order(int32_t n, const std::vector<int32_t> &xadj,
+               const std::vector<int32_t> &adj, std::vector<int32_t> &perm) {
+  perm.assign(n, 0);
+  std::vector<char> mask(n, 1), seen(n, 0);
+  std::vector<int32_t> xls(n + 2), deg(n, 0);
+  int num = 0;
+  for (int i = 0; i < n && num < n; i++) {
+    if (!mask[i]) continue;
+    int32_t *ls = perm.data() + num;
+    int root = pseudo_peripheral(i, xadj, adj, mask, ls, xls);
+    // masked degrees of the component (degree, Reord.f:355-435)
+    int size = 1;
+    ls[0] = root;
+    seen[root] = 1;
+    for (int h = 0; h < size; h++) {
+      int v = ls[h], d = 0;
+      for (int k = xadj[v]; k < xadj[v + 1]; k++) {
+        int w = adj[k];
+        if (!mask[w]) continue;
+        d++;
+        if (!seen[w]) {
+          seen[w] = 1;
+          ls[size++] = w;
+        }
+      }
+      deg[v] = d;
+    }
+    for (int h = 0; h < size; h++) seen[ls[h]] = 0;
+    // Cuthill-McKee numbering (rcm, Reord.f:170-265)
+    mask[root] = 0;
+    ls[0] = root;
+    int last = 1;  // one past the last numbered node
+    for (int h = 0; h < last; h++) {
+      int v = ls[h];
+      int first_new = last;
+      for (int k = xadj[v]; k < xadj[v + 1]; k++) {
+        int w = adj[k];
+        if (!mask[w]) continue;
+        mask[w] = 0;
+        ls[last++] = w;
+      }
+      // stable insertion sort of the new neighbours by degree
+      for (int a = first_new + 1; a < last; a++) {
+        int w = ls[a], b = a - 1;
+        while (b >= first_new && deg[ls[b]] > deg[w]) {
+          ls[b + 1] = ls[b];
+          b--;
+        }
+        ls[b + 1] = w;
+      }
+    }
+    std::reverse(ls, ls + size);
+    num += size;
+  }
+}
+
+// Equation numbering (numeq, Numeq.f:139-192): nodes visited in perm order,
+// the free dofs of a node numbered consecutively in dof order.
+// bc(ndf,nnode): nonzero = constrained.  id gets 1-based numbers, 0 = fixed.
+int32_t number_equations(const Mesh &m, const std::vector<int32_t> &perm,
+                         const int32_t *bc, std::vector<int32_t> &id) {
+  id.assign((size_t)m.ndf * m.nnode, 0);
+  int32_t neq = 0;
+  for (int k = 0; k < m.nnode; k++) {
+    int v = perm[k];
+    for (int d = 0; d < m.ndf; d++) {
+      size_t q = (size_t)v * m.ndf + d;
+      id[q] = bc[q] == 0 ? ++neq : 0;
+    }
+  }
+  return neq;
+}
+
+// Lower CSRC pattern (csrstruct/csria/csrja lower-only + sortgraph,
+// Csr.f:13-305): row r holds, ascending, every equation c < r of the same
+// node or of an adjacent node.  Since a node's free equations are
+// consecutive and the blocks of different nodes are disjoint, each row is the
+// concatenation of whole blocks of lower adjacent nodes (sorted by their
+// first equation) followed by the node's own lower equations.
+void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> &xadj,
+                  const std::vector<int32_t> &adj, std::vector<int32_t> &ia,
+                  std::vector<int32_t> &ja) {
+  const int ndf = m.ndf;
+  const int32_t neq = s.neq;
+  std::vector<int32_t> first(m.nnode, 0), nfree(m.nnode, 0);
+  for (int v = 0; v < m.nnode; v++) {
+    int f = 0, c = 0;
+    for (int d = 0; d < ndf; d++) {
+      int q = s.id[(size_t)v * ndf + d];
+      if (q > 0) {
+        if (!c) f = q;
+        c++;
+      }
+    }
+    first[v] = f;
+    nfree[v] = c;
+  }
+  ia.assign(neq + 1, 0);
+  // row lengths
+  std::vector<int32_t> lower_cols(m.nnode, 0);
+  for (int v = 0; v < m.nnode; v++) {
+    if (!nfree[v]) continue;
+    int32_t cnt = 0;
+    for (int k = xadj[v]; k < xadj[v + 1]; k++) {
+      int w = adj[k];
+      if (nfree[w] && first[w] < first[v]) cnt += nfree[w];
+    }
+    lower_cols[v] = cnt;
+    for (int d = 0; d < nfree[v]; d++) ia[first[v] - 1 + d + 1] = cnt + d;
+  }
+  ia[0] = 1;
+  for (int r = 0; r < neq; r++) ia[r + 1] += ia[r];
+  ja.assign((size_t)ia[neq] - 1, 0);
+  std::vector<std::pair<int32_t, int32_t>> blocks;
+  for (int v = 0; v < m.nnode; v++) {
+    if (!nfree[v]) continue;
+    blocks.clear();
+    for (int k = xadj[v]; k < xadj[v + 1]; k++) {
+      int w = adj[k];
+      if (nfree[w] && first[w] < first[v]) blocks.emplace_back(first[w], nfree[w]);
+    }
+    std::sort(blocks.begin(), blocks.end());
+    for (int d = 0; d < nfree[v]; d++) {
+      int32_t r = first[v] + d;  // 1-based row
+      int64_t p = ia[r - 1] - 1;
+      for (auto &b : blocks)
+        for (int t = 0; t < b.second; t++) ja[p++] = b.first + t;
+      for (int t = 0; t < d; t++) ja[p++] = first[v] + t;
+    }
+  }
+}
+
+// What the kernels need beyond ia/ja/id:
+//  * the transposed index: for every equation c the lower-part entries in
+//    column c (their rows jat and positions pt in al), ascending by row;
+//  * a greedy element colouring in which no two elements of a colour share a
+//    node (so colour-ordered assembly needs no atomics), elements grouped per
+//    colour and element type;
+//  * the slot map: for each element and each unordered pair of its nodes
+//    {a, b} with free dofs, the offset within the row of the higher node of
+//    the lower node's first column (identical for every dof row of that node).
+void derive_structure(const Mesh &m, Structure &s) {
+  const int32_t neq = s.neq;
+  const int64_t nad = s.nad;
+  // ---- transposed index (counting sort by column)
+  s.iat.assign(neq + 1, 0);
+  for (int64_t k = 0; k < nad; k++) s.iat[s.ja[k]]++;  // ja is 1-based: col c -> iat[c]
+  for (int c = 0; c < neq; c++) s.iat[c + 1] += s.iat[c];
+  s.jat.assign(nad, 0);
+  s.pt.assign(nad, 0);
+  {
+    std::vector<int32_t> fill(s.iat.begin(), s.iat.end() - 1);
+    for (int r = 0; r < neq; r++)
+      for (int32_t k = s.ia[r] - 1; k < s.ia[r + 1] - 1; k++) {
+        int c = s.ja[k] - 1;
+        int32_t q = fill[c]++;
+        s.jat[q] = r;
+        s.pt[q] = k;
+      }
+  }
+  // ---- element colouring
+  const int nen1 = m.nen + 1;
+  std::vector<int32_t> color(m.numel, -1);
+  std::vector<std::vector<uint64_t>> used;  // per node, bit per colour (64 per word)
+  int words = 1;
+  used.assign(m.nnode, std::vector<uint64_t>(words, 0));
+  int ncolors = 0;
+  for (int el = 0; el < m.numel; el++) {
+    const int32_t *c = &m.ix[(size_t)el * nen1];
+    int iel = m.ie[c[m.nen] - 1];
+    int nv = elem_nodes(iel);
+    int chosen = -1;
+    for (int w = 0; chosen < 0; w++) {
+      if (w == words) {
+        words++;
+        for (auto &u : used) u.push_back(0);
+      }
+      uint64_t busy = 0;
+      for (int a = 0; a < nv; a++) busy |= used[c[a] - 1][w];
+      if (~busy) chosen = w * 64 + __builtin_ctzll(~busy);
+    }
+    color[el] = chosen;
+    ncolors = std::max(ncolors, chosen + 1);
+    for (int a = 0; a < nv; a++) used[c[a] - 1][chosen / 64] |= 1ull << (chosen % 64);
+  }
+  s.ncolors = ncolors;
+  // group by (colour, element type), elements ascending inside a group
+  s.elem_order.resize(m.numel);
+  std::iota(s.elem_order.begin(), s.elem_order.end(), 0);
+  auto type_of = [&](int el) { return m.ie[m.ix[(size_t)el * nen1 + m.nen] - 1]; };
+  std::stable_sort(s.elem_order.begin(), s.elem_order.end(), [&](int a, int b) {
+    if (color[a] != color[b]) return color[a] < color[b];
+    return type_of(a) < type_of(b);
+  });
+  s.segments.clear();
+  s.color_of_segment.clear();
+  for (int i = 0; i < m.numel;) {
+    int el = s.elem_order[i];
+    int c = color[el], t = type_of(el), j = i;
+    while (j < m.numel && color[s.elem_order[j]] == c && type_of(s.elem_order[j]) == t) j++;
+    s.segments.push_back({t, i, j});
+    s.color_of_segment.push_back(c);
+    i = j;
+  }
+  // ---- slot map
+  const int nen = m.nen;
+  s.npairs = nen * (nen - 1) / 2;
+  s.slot.assign((size_t)s.npairs * m.numel, -1);
+  std::vector<int32_t> first(m.nnode, 0);
+  for (int v = 0; v < m.nnode; v++)
+    for (int d = m.ndf - 1; d >= 0; d--) {
+      int q = s.id[(size_t)v * m.ndf + d];
+      if (q > 0) first[v] = q;  // smallest free equation of the node
+    }
+  for (int t = 0; t < m.numel; t++) {
+    int el = s.elem_order[t];
+    const int32_t *c = &m.ix[(size_t)el * nen1];
+    int nv = elem_nodes(type_of(el));
+    int pair = 0;
+    for (int a = 0; a < nen; a++)
+      for (int b = a + 1; b < nen; b++, pair++) {
+        if (a >= nv || b >= nv) continue;
+        int va = c[a] - 1, vb = c[b] - 1;
+        if (!first[va] || !first[vb] || va == vb) continue;
+        int hi = first[va] > first[vb] ? va : vb;
+        int lo = hi == va ? vb : va;
+        int32_t r = first[hi] - 1;  // 0-based row of the higher node's first dof
+        const int32_t *rb = s.ja.data() + (s.ia[r] - 1);
+        const int32_t *re = s.ja.data() + (s.ia[r + 1] - 1);
+        const int32_t *pos = std::lower_bound(rb, re, first[lo]);
+        ELX_REQUIRE(pos != re && *pos == first[lo], ELX_ERR_ARG,
+                    "CSRC pattern does not contain an element's node pair");
+        s.slot[(size_t)pair * m.numel + t] = (int32_t)(pos - rb);
+      }
+  }
+}
+
+}  // namespace elx

@@ -1,0 +1,188 @@
+/*
+ * elastic_gb300.h -- C ABI of the GB300 (sm_103a) linear-elasticity solve
+ * library: element stiffness integration for TRIA3/QUAD4/TETRA4/HEXA8,
+ * assembly into CSRC storage, the CSRC matrix-vector product and Jacobi-PCG
+ * (with BiCGSTAB and GMRES on the same kernels).
+ *
+ * It replaces two calls of the Fortran driver of lmn-labest/Elastic:
+ *   pform_mec(..., lhs=.true., rhs=.true., isw=2, ...)   mef/src/Pform.f:1-11,
+ *                                                         called at Main.f:791-802
+ *   solv(neq,nad,ip,ja,ad,au,al,m,b,x,tol,maxit,ngram,...) mef/src/Solv.f:13-15,
+ *                                                         called at Main.f:820-826
+ * Everything else in the driver (deck reading, RCM, numeq, load vectors,
+ * output) stays where it is.
+ *
+ * Conventions (the reference's): every array is passed by plain pointer; all
+ * index CONTENTS are 1-based (node, material, equation numbers, ia/ja
+ * positions); multi-dimensional arrays are Fortran column-major, e.g.
+ * ix(nen+1,numel) with the material number in the last row, x(ndm,nnode),
+ * id(ndf,nnode), e(prop,numat), u(ndf,nnode).  Integers are int32 unless
+ * stated; reals are double.  CSRC = diagonal ad(neq) + strict lower part in CSR
+ * (ia(neq+1), ja(nad), al(nad)); the upper part is al mirrored.
+ *
+ * Errors: every call returns ELX_OK (0) or an ELX_ERR_* code and never exits
+ * the process; elx_last_error() returns the message of the context's last
+ * failure.  The Fortran glue calls stop_mef on a non-zero status, which keeps
+ * the reference's behaviour (Paralelo.f:1123-1130).
+ *
+ * Threading: one context per host thread; calls are synchronous to the host
+ * unless named *_async.  Device memory is owned by the context.
+ */
+#ifndef ELASTIC_GB300_H
+#define ELASTIC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define ELX_OK 0
+#define ELX_ERR_ZERO_DIAG 1      /* ad(i) == 0 (Iters.f:337-342)              */
+#define ELX_ERR_NO_CONVERGENCE 2 /* maxit reached (Iters.f:429-431)           */
+#define ELX_ERR_BAD_DET 3        /* element det <= 1e-14 (Elmlib.f:1826-1829) */
+#define ELX_ERR_OOM 4            /* device allocation or HBM budget           */
+#define ELX_ERR_TIMEOUT 5        /* a bounded device wait gave up             */
+#define ELX_ERR_ARG 6            /* invalid argument                          */
+#define ELX_ERR_BAD_ELEMENT 7    /* unknown element type (Elmlib.f:151-153)   */
+#define ELX_ERR_CUDA 8           /* CUDA runtime error                        */
+#define ELX_ERR_STATE 9          /* call out of order (e.g. solve before mesh)*/
+
+/* solver codes (the reference's `solver` variable, Main.f:177-198) */
+#define ELX_SOLVER_PCG 1
+#define ELX_SOLVER_GMRES 2
+#define ELX_SOLVER_BICGSTAB 4
+
+/* precision of the Krylov iteration */
+#define ELX_PREC_FP64 0  /* everything in FP64, as the reference          */
+#define ELX_PREC_MIXED 1 /* FP32 inner PCG inside FP64 iterative refinement */
+
+typedef struct elx_ctx elx_ctx;
+
+typedef struct elx_opts {
+  int32_t device;     /* CUDA device ordinal                                */
+  int32_t verbose;    /* 0 silent                                            */
+  int64_t hbm_budget; /* bytes the context may allocate; 0 = no limit        */
+} elx_opts;
+
+/* Post-solve diagnostics, the fields PCG prints at Iters.f:473-490. */
+typedef struct elx_info {
+  int32_t iters;      /* Krylov iterations (GMRES: inner steps)              */
+  int32_t status;     /* ELX_* status of this solve                          */
+  double xkx;         /* x . K x                                             */
+  double norm_x;      /* ||x||_2                                             */
+  double norm_r;      /* ||b - K x||_2                                       */
+  double norm_m_r;    /* ||b - K x||_M, M = diag(K)^-1                       */
+  double conv;        /* stopping threshold tol * ||b||_M (GMRES/BiCGSTAB: 2-norm) */
+  double seconds;     /* wall time of the solve on the device                */
+  double mflops;      /* flop_cg(neq,nad,iters,2) / seconds (Matvec.f:1499) */
+  int32_t refinements;/* mixed precision: outer FP64 refinement steps        */
+  int32_t inner_iters;/* mixed precision: total FP32 inner iterations        */
+} elx_info;
+
+/* ---- context ---------------------------------------------------------- */
+int elx_create(elx_ctx **out, const elx_opts *opts);
+void elx_destroy(elx_ctx *ctx);
+const char *elx_last_error(const elx_ctx *ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or
+ * order device work around the library's. */
+void *elx_stream(elx_ctx *ctx);
+/* Bytes of device memory the context holds. */
+int64_t elx_device_bytes(const elx_ctx *ctx);
+/* Number of this library's kernels the context has launched so far
+ * (a CUDA graph launch counts the kernels it contains). */
+int64_t elx_kernel_launches(const elx_ctx *ctx);
+const char *elx_version(void);
+
+/* ---- mesh and structure ------------------------------------------------ */
+/* Mesh arrays as read by rdat (Rdata.f:1-740).  ix(nen+1,numel); x(ndm,nnode);
+ * ie(numat) element type per material (2,3 TRIA3; 4,5 QUAD4; 6 TETRA4;
+ * 7 HEXA8); e(prop,numat) with E, nu, thickness in rows 1..3.  Copies them to
+ * the device.  Element types are checked here (ELX_ERR_BAD_ELEMENT). */
+int elx_set_mesh(elx_ctx *ctx, int32_t ndm, int32_t ndf, int32_t nen,
+                 int32_t numel, int32_t nnode, const int32_t *ix,
+                 const double *x, const int32_t *ie, const double *e,
+                 int32_t prop, int32_t numat);
+
+/* Structure computed by the caller, as the reference driver does
+ * (reord Reord.f:1, numeq Numeq.f:139, csrstruct Csr.f:13 lower-only):
+ * id(ndf,nnode) equation numbers (0 = constrained), ia(neq+1), ja(nad).
+ * The library derives the transposed index, the element colouring and the
+ * per-element slot map from them and uploads everything once. */
+int elx_set_structure(elx_ctx *ctx, int32_t neq, int64_t nad,
+                      const int32_t *id, const int32_t *ia, const int32_t *ja);
+
+/* Structure computed by the library on the host from the mesh: node graph
+ * (Graph.f:20), RCM when reorder != 0 (Reord.f:1), equation numbering
+ * (Numeq.f:139) from bc(ndf,nnode) with 1 = constrained, and the lower CSRC
+ * pattern (Csr.f:13).  Same output as the reference, bit for bit. */
+int elx_build_structure(elx_ctx *ctx, const int32_t *bc, int32_t reorder);
+
+/* Host-only form of elx_build_structure, usable without a GPU (for example
+ * by a driver that replaces reord/numeq/csrstruct, Main.f:412-491): builds
+ * the structure into a host handle; read it back with the two getters.
+ * ix, ie as for elx_set_mesh, bc(ndf,nnode) with 1 = constrained. */
+typedef struct elx_host_structure elx_host_structure;
+int elx_host_structure_create(elx_host_structure **out, int32_t ndm, int32_t ndf,
+                              int32_t nen, int32_t numel, int32_t nnode,
+                              const int32_t *ix, const int32_t *ie, int32_t numat,
+                              const int32_t *bc, int32_t reorder);
+int elx_host_structure_sizes(const elx_host_structure *h, int32_t *neq,
+                             int64_t *nad);
+int elx_host_structure_get(const elx_host_structure *h, int32_t *perm,
+                           int32_t *id, int32_t *ia, int32_t *ja);
+void elx_host_structure_destroy(elx_host_structure *h);
+
+/* Sizes and copies of the structure (any pointer may be NULL). */
+int elx_get_sizes(const elx_ctx *ctx, int32_t *neq, int64_t *nad,
+                  int32_t *ncolors);
+int elx_get_structure(const elx_ctx *ctx, int32_t *perm, int32_t *id,
+                      int32_t *ia, int32_t *ja);
+
+/* ---- assembly: pform_mec(isw=2, lhs=.true., rhs=.true.) ----------------- */
+/* u(ndf,nnode) current displacements (prescribed values in constrained dofs),
+ * b0(neq) load vector.  Forms K (ad, al, device-resident) and
+ * b_out = b0 - K_e u_e summed over elements (Assbly.f:116-118).  ad_out and
+ * al_out are optional host copies (NULL = keep on the device only). */
+int elx_assemble(elx_ctx *ctx, const double *u, const double *b0,
+                 double *b_out, double *ad_out, double *al_out);
+
+/* ---- solve: solv(...) -------------------------------------------------- */
+/* Solves K x = b with the resident K.  solver: ELX_SOLVER_*; precision:
+ * ELX_PREC_*; tol, maxit, ngram as in the reference (Main.f:177-198).
+ * b and x are host arrays of length neq; x need not be initialised (x0 = 0). */
+int elx_solve(elx_ctx *ctx, int32_t solver, int32_t precision, double tol,
+              int32_t maxit, int32_t ngram, const double *b, double *x,
+              elx_info *info);
+
+/* update_mec (Predict.f:183-209): u(j,i) = x(id(j,i)) for free dofs. */
+int elx_update(elx_ctx *ctx, const double *x, double *u);
+
+/* ---- lower-level calls on resident data (benchmarks, tests) ------------ */
+/* y = K x with the resident K (matvec_csrcsym1, Matvec.f:528-621).
+ * precision ELX_PREC_FP64 or ELX_PREC_MIXED (FP32 values and vectors). */
+int elx_spmv(elx_ctx *ctx, int32_t precision, const double *x, double *y);
+
+/* Upload the matrix directly (ad(neq), al(nad)) instead of assembling it. */
+int elx_set_matrix(elx_ctx *ctx, const double *ad, const double *al);
+
+/* Device-resident steps, no host copies: assembly from the resident u and b0
+ * (elx_set_state), a solve from the resident b into the resident x, and
+ * `reps` SpMVs y = K x on resident vectors.  All are stream-ordered on
+ * elx_stream(ctx) and return once enqueued, except elx_solve_resident which
+ * waits for convergence. */
+int elx_set_state(elx_ctx *ctx, const double *u, const double *b0);
+int elx_assemble_resident(elx_ctx *ctx);
+int elx_solve_resident(elx_ctx *ctx, int32_t solver, int32_t precision,
+                       double tol, int32_t maxit, int32_t ngram,
+                       elx_info *info);
+int elx_spmv_resident(elx_ctx *ctx, int32_t precision, int32_t reps);
+int elx_get_solution(elx_ctx *ctx, double *x);
+int elx_get_rhs(elx_ctx *ctx, double *b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ELASTIC_GB300_H */

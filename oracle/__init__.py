@@ -1,0 +1,317 @@
+"""CPU oracle for the Elastic linear-elasticity solve path.
+
+TEST INFRASTRUCTURE ONLY: the tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` use this module to check (or to time, as the
+reference's own CPU path) the CUDA library.  The product package
+``elastic_gb300`` never imports it.
+
+The numerics live in ``elx_oracle.c`` (a restatement of the reference's
+Fortran routines, each citing its file:line); this module is a thin ctypes
+wrapper that also replays the reference driver's ``solvm`` sequence
+(mef/src/Main.f:718-849).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SO = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+I32P = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+F64P = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+
+STATUS = {0: "ok", 1: "zero diagonal", 2: "no convergence", 3: "bad determinant",
+          4: "out of memory", 6: "bad argument", 7: "bad element type"}
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, what=""):
+        super().__init__(f"oracle: {STATUS.get(code, code)} {what}".strip())
+        self.code = code
+
+
+class Info(C.Structure):
+    _fields_ = [("iters", C.c_int), ("status", C.c_int), ("xkx", C.c_double),
+                ("norm_x", C.c_double), ("norm_r", C.c_double),
+                ("norm_m_r", C.c_double), ("conv", C.c_double),
+                ("seconds", C.c_double), ("mflops", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def build():
+    """Compile oracle/_build/liboracle.so with the committed Makefile."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_SO) or (
+                os.path.getmtime(_SO) < os.path.getmtime(os.path.join(_HERE, "elx_oracle.c"))):
+            build()
+        L = C.CDLL(_SO)
+        L.orc_graph.restype = C.c_int
+        L.orc_graph.argtypes = [I32P, C.c_int, C.c_int, C.c_int, I32P, I32P, C.c_int]
+        L.orc_reord.argtypes = [I32P, C.c_int, C.c_int, C.c_int, I32P]
+        L.orc_numeq.argtypes = [I32P, I32P, C.c_int, C.c_int]
+        L.orc_csr_ia.restype = C.c_longlong
+        L.orc_csr_ia.argtypes = [I32P, I32P, I32P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, I32P]
+        L.orc_csr_ja.argtypes = [I32P, I32P, I32P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, I32P, I32P]
+        L.orc_element_stiffness.argtypes = [C.c_int, F64P, F64P, C.c_int, F64P]
+        L.orc_pform_k.argtypes = [I32P, I32P, F64P, C.c_int, F64P, I32P, I32P, I32P, F64P, F64P,
+                                  F64P, F64P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                  C.c_int, C.c_longlong, C.c_int, C.c_int, C.POINTER(C.c_int)]
+        L.orc_pform_edge_loads.argtypes = [I32P, I32P, F64P, I32P, I32P, F64P, F64P, C.c_int,
+                                           C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]
+        L.orc_pload.argtypes = [I32P, F64P, F64P, F64P, C.c_int, C.c_int]
+        L.orc_update.argtypes = [I32P, F64P, F64P, C.c_int, C.c_int]
+        L.orc_matvec_csrcsym1.argtypes = [C.c_int, I32P, I32P, F64P, F64P, F64P, F64P]
+        L.orc_dot.restype = C.c_double
+        L.orc_dot.argtypes = [F64P, F64P, C.c_int]
+        L.orc_flop_cg.restype = C.c_double
+        L.orc_flop_cg.argtypes = [C.c_int, C.c_longlong, C.c_int]
+        L.orc_pre_diag.argtypes = [F64P, F64P, C.c_int]
+        sol = [C.c_int, C.c_longlong, I32P, I32P, F64P, F64P, F64P, F64P]
+        L.orc_pcg.argtypes = sol + [C.c_double, C.c_int, C.POINTER(Info)]
+        L.orc_pbicgstab.argtypes = sol + [C.c_double, C.c_int, C.POINTER(Info)]
+        L.orc_gmres.argtypes = sol + [C.c_int, C.c_double, C.c_int, C.POINTER(Info)]
+        L.orc_pcg_omp.argtypes = sol + [C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(Info)]
+        L.orc_matvec_csrcsym_omp.argtypes = [C.c_int, I32P, I32P, F64P, F64P, F64P, F64P, C.c_int,
+                                             C.c_int, C.POINTER(C.c_double)]
+        L.orc_max_threads.restype = C.c_int
+        L.orc_colormsh.argtypes = [I32P, C.c_int, C.c_int, C.c_int, C.c_int, I32P, I32P, C.c_int]
+        L.orc_pform_k_omp.argtypes = [I32P, I32P, F64P, C.c_int, F64P, I32P, I32P, I32P, F64P,
+                                      F64P, F64P, F64P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_int, C.c_int, C.c_longlong, I32P, I32P, C.c_int,
+                                      C.c_int, C.POINTER(C.c_int)]
+        _lib = L
+    return _lib
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+@dataclass
+class Structure:
+    """Equation numbering and CSRC pattern, 1-based as in the reference."""
+    perm: np.ndarray   # (nnode,) old node at new position k (Reord.f)
+    id: np.ndarray     # (nnode, ndf) equation numbers, 0 = constrained
+    neq: int
+    nad: int
+    ia: np.ndarray     # (neq+1,) 1-based
+    ja: np.ndarray     # (nad,) 1-based, ascending per row
+
+
+def graph(mesh):
+    L = lib()
+    ix = _i32(mesh.ix)
+    ip = np.zeros(mesh.nnode + 1, np.int32)
+    cap = mesh.numel * mesh.nen * (mesh.nen - 1) + 1
+    adj = np.zeros(cap, np.int32)
+    n = L.orc_graph(ix, mesh.nnode, mesh.numel, mesh.nen, ip, adj, cap)
+    if n < 0:
+        raise OracleError(-n, "graph")
+    return ip, adj[:n].copy()
+
+
+def structure(mesh, reorder=True) -> Structure:
+    """reord (Reord.f:1) + numeq (Numeq.f:139) + csrstruct lower-only (Csr.f:13)."""
+    L = lib()
+    ix = _i32(mesh.ix)
+    if reorder:
+        perm = np.zeros(mesh.nnode, np.int32)
+        st = L.orc_reord(ix, mesh.nnode, mesh.numel, mesh.nen, perm)
+        if st:
+            raise OracleError(st, "reord")
+    else:
+        perm = np.arange(1, mesh.nnode + 1, dtype=np.int32)
+    idm = _i32(mesh.id).copy()
+    neq = L.orc_numeq(idm, perm, mesh.nnode, mesh.ndf)
+    ia = np.zeros(neq + 1, np.int32)
+    nad = L.orc_csr_ia(idm, perm, ix, mesh.nnode, mesh.numel, mesh.nen, mesh.ndf, neq, ia)
+    if nad < 0:
+        raise OracleError(-nad, "csria")
+    ja = np.zeros(max(nad, 1), np.int32)
+    st = L.orc_csr_ja(idm, perm, ix, mesh.nnode, mesh.numel, mesh.nen, mesh.ndf, neq, ia, ja)
+    if st:
+        raise OracleError(st, "csrja")
+    return Structure(perm=perm, id=idm, neq=int(neq), nad=int(nad), ia=ia, ja=ja[:nad])
+
+
+def element_stiffness(iel, e, xl):
+    """One element matrix s(nst,nst) as a numpy (nst, nst) array s[row, col]."""
+    L = lib()
+    nst = {2: 6, 3: 6, 4: 8, 5: 8, 6: 12, 7: 24}[iel]
+    ndm = 2 if iel <= 5 else 3
+    s = np.zeros(nst * nst)
+    ev = np.zeros(15)
+    ev[:len(e)] = e
+    st = L.orc_element_stiffness(iel, ev, _f64(np.asarray(xl).reshape(-1)), ndm, s)
+    if st:
+        raise OracleError(st, "element")
+    return s.reshape(nst, nst).T.copy()  # column-major -> [row, col]
+
+
+def assemble(mesh, s: Structure, u=None, b0=None, lhs=True, rhs=True):
+    """pform_mec(isw=2) (Pform.f:1-254 + Assbly.f:66-146): returns (ad, al, b)
+    with b = b0 - K u (rows of free dofs)."""
+    L = lib()
+    ad = np.zeros(s.neq)
+    al = np.zeros(max(s.nad, 1))
+    b = _f64(b0).copy() if b0 is not None else np.zeros(s.neq)
+    u = _f64(u) if u is not None else np.zeros((mesh.nnode, mesh.ndf))
+    bad = C.c_int(0)
+    st = L.orc_pform_k(_i32(mesh.ix), _i32(mesh.ie), _f64(mesh.e), mesh.e.shape[1],
+                       _f64(mesh.x), s.id, s.ia, _i32(s.ja) if s.nad else np.zeros(1, np.int32),
+                       al, ad, b, u, mesh.numel, mesh.nen, mesh.nen, mesh.ndf, mesh.ndm,
+                       s.neq, s.nad, int(lhs), int(rhs), C.byref(bad))
+    if st:
+        raise OracleError(st, f"element {bad.value}")
+    return ad, al[:s.nad], b
+
+
+def colormsh(mesh):
+    """coloredmesh with omp_elmt (Colormsh.f:9-308): (elcolor, colorg)."""
+    elcolor = np.zeros(mesh.numel, np.int32)
+    colorg = np.zeros(2 * 200, np.int32)
+    nc = lib().orc_colormsh(_i32(mesh.ix), mesh.nnode, mesh.numel, mesh.nen, mesh.nen,
+                            elcolor, colorg, 200)
+    if nc < 0:
+        raise OracleError(-nc, "colormsh")
+    return elcolor, colorg[:2 * nc].copy()
+
+
+def assemble_omp(mesh, s: Structure, u=None, b0=None, nthreads=None, colors=None):
+    """pform_mec(isw=2) with the OpenMP colour loop (Pform.f:108-183)."""
+    L = lib()
+    nth = nthreads or L.orc_max_threads()
+    elcolor, colorg = colors if colors is not None else colormsh(mesh)
+    ad = np.zeros(s.neq)
+    al = np.zeros(max(s.nad, 1))
+    b = _f64(b0).copy() if b0 is not None else np.zeros(s.neq)
+    u = _f64(u) if u is not None else np.zeros((mesh.nnode, mesh.ndf))
+    bad = C.c_int(0)
+    st = L.orc_pform_k_omp(_i32(mesh.ix), _i32(mesh.ie), _f64(mesh.e), mesh.e.shape[1],
+                           _f64(mesh.x), s.id, s.ia, _i32(s.ja), al, ad, b, u, mesh.numel,
+                           mesh.nen, mesh.nen, mesh.ndf, mesh.ndm, s.neq, s.nad, elcolor,
+                           colorg, colorg.shape[0] // 2, nth, C.byref(bad))
+    if st:
+        raise OracleError(st, f"element {bad.value}")
+    return ad, al[:s.nad], b
+
+
+def loads(mesh, s: Structure):
+    """pload_mec (Pload.f:2-58) then pform_mec isw=4 edge loads: (b0, u)."""
+    L = lib()
+    b0 = np.zeros(s.neq)
+    u = np.zeros((mesh.nnode, mesh.ndf))
+    L.orc_pload(s.id, _f64(mesh.f), u, b0, mesh.nnode, mesh.ndf)
+    if mesh.eload is not None:
+        bad = C.c_int(0)
+        st = L.orc_pform_edge_loads(_i32(mesh.ix), _i32(mesh.ie), _f64(mesh.x), s.id,
+                                    _i32(mesh.eload), _f64(mesh.loadvec), b0, mesh.numel,
+                                    mesh.nen, mesh.ndf, mesh.ndm, s.neq, C.byref(bad))
+        if st:
+            raise OracleError(st, f"edge load element {bad.value}")
+    return b0, u
+
+
+def matvec(s: Structure, ad, al, x):
+    """matvec_csrcsym1 (Matvec.f:528-621)."""
+    y = np.zeros(s.neq)
+    lib().orc_matvec_csrcsym1(s.neq, s.ia, _i32(s.ja) if s.nad else np.zeros(1, np.int32),
+                              _f64(ad), _f64(al) if s.nad else np.zeros(1), _f64(x), y)
+    return y
+
+
+def _solve(fn, s, ad, al, b, *extra):
+    x = np.zeros(s.neq)
+    info = Info()
+    ja = _i32(s.ja) if s.nad else np.zeros(1, np.int32)
+    alv = _f64(al) if s.nad else np.zeros(1)
+    st = fn(s.neq, s.nad, s.ia, ja, _f64(ad), alv, _f64(b), x, *extra, C.byref(info))
+    return x, info.as_dict()
+
+
+def pcg(s, ad, al, b, tol=1e-11, maxit=10000):
+    """pcg (Iters.f:252-524) with the Jacobi preconditioner of Solv.f:65-69."""
+    return _solve(lib().orc_pcg, s, ad, al, b, tol, maxit)
+
+
+def pcg_omp(s, ad, al, b, tol=1e-11, maxit=10000, nthreads=None, stop_at_maxit=False):
+    """pcg_omp (Iters_omp.f:17-334) with matvec_csrcsym_omp."""
+    nth = nthreads or lib().orc_max_threads()
+    return _solve(lib().orc_pcg_omp, s, ad, al, b, tol, maxit, nth, int(stop_at_maxit))
+
+
+def pbicgstab(s, ad, al, b, tol=1e-11, maxit=10000):
+    """pbicgstab (Iters.f:1079-1349)."""
+    return _solve(lib().orc_pbicgstab, s, ad, al, b, tol, maxit)
+
+
+def gmres(s, ad, al, b, k=50, tol=1e-11, maxit=10000):
+    """gmres (Iters.f:528-808); maxit counts restart cycles."""
+    return _solve(lib().orc_gmres, s, ad, al, b, k, tol, maxit)
+
+
+def matvec_omp(s, ad, al, x, nthreads=None, reps=1):
+    """matvec_csrcsym_omp (Matvec_omp.f:150-245); returns (y, seconds)."""
+    nth = nthreads or lib().orc_max_threads()
+    y = np.zeros(s.neq)
+    sec = C.c_double(0)
+    st = lib().orc_matvec_csrcsym_omp(s.neq, s.ia, _i32(s.ja), _f64(ad), _f64(al), _f64(x), y,
+                                      nth, reps, C.byref(sec))
+    if st:
+        raise OracleError(st, "matvec_omp")
+    return y, sec.value
+
+
+def update(s: Structure, xsol, u):
+    """update_mec (Predict.f:183-209)."""
+    u = _f64(u).copy()
+    lib().orc_update(s.id, _f64(xsol), u, u.shape[0], u.shape[1])
+    return u
+
+
+def solvm(mesh, tol=1e-11, maxit=10000, maxnlit=2, nl_tol=1e-4, solver="pcg",
+          reorder=True, s=None):
+    """Replay of the reference driver's solvm macro (Main.f:718-849) for a
+    linear problem: loads, then up to maxnlit passes of assemble -> residual
+    test -> solve -> update.  Returns (u, info of the solve, structure, ad, al)."""
+    s = s or structure(mesh, reorder)
+    b0, u = loads(mesh, s)
+    resid0 = 0.0
+    info = None
+    ad = al = None
+    for i in range(1, maxnlit + 1):
+        ad, al, b = assemble(mesh, s, u, b0)
+        resid = float(np.sqrt(lib().orc_dot(b, b, s.neq)))
+        if i == 1:
+            resid0 = max(resid0, resid)
+        if resid0 > 0 and resid / resid0 < nl_tol:
+            break
+        if solver == "pcg":
+            x, info = pcg(s, ad, al, b, tol, maxit)
+        elif solver == "bicgstab":
+            x, info = pbicgstab(s, ad, al, b, tol, maxit)
+        elif solver == "gmres":
+            x, info = gmres(s, ad, al, b, 50, tol, maxit)
+        else:
+            raise ValueError(solver)
+        if info["status"] != 0:
+            raise OracleError(info["status"], "solve")
+        u = update(s, x, u)
+    return u, info, s, ad, al
