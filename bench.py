@@ -269,6 +269,41 @@ def run_ours(args, dist: Dist):
     return out
 
 
+def run_spmv_only(args):
+    """Assemble the workload once, then time `steps` SpMVs (after `warmup`)."""
+    import torch
+
+    import elastic_gb300 as E
+
+    mesh = make_workload()
+    ctx = E.Context(device=0)
+    ctx.set_mesh(mesh)
+    neq, nad, _ = ctx.build_structure(True)
+    st = ctx.structure()
+    b0, u0 = E.pload(mesh, st.id)
+    ctx.set_state(u0, b0)
+    ctx.assemble_resident()
+    try:  # a short solve leaves a non-trivial search direction p behind
+        ctx.solve_resident(tol=1e-2, maxit=50)
+    except E.ElasticError:
+        pass
+    ext = torch.cuda.ExternalStream(ctx.stream, device=0)
+    ctx.spmv_resident(reps=args.warmup)
+    torch.cuda.synchronize(0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    ctx.spmv_resident(reps=args.steps)
+    e1.record(ext)
+    torch.cuda.synchronize(0)
+    ms = e0.elapsed_time(e1) / args.steps
+    byts = 12 * nad + 28 * neq
+    peak, kind = measured_peak()
+    ctx.close()
+    return {"mode": "spmv", "neq": neq, "nad": nad, "spmv_ms": ms,
+            "spmv_gbs": byts / (ms * 1e-3) / 1e9, "frac": byts / (ms * 1e-3) / 1e9 / peak,
+            "peak": peak, "peak_kind": kind}
+
+
 # ------------------------------------------------------------------ CPU side
 def cpu_baseline(mesh, st, b0, u0, full_iters=None, sample_iters=300, nthreads=None):
     """The reference's OpenMP CPU path (oracle restatement of pform_mec's
@@ -348,11 +383,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", choices=["full", "spmv"], default="full",
+                    help="spmv: only the FP64 SpMV of the workload (for profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = Dist(args.impl)
     try:
-        out = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+        if args.impl == "reference":
+            out = run_reference(args, dist)
+        elif args.mode == "spmv":
+            out = run_spmv_only(args)
+        else:
+            out = run_ours(args, dist)
     finally:
         dist.close()
     if out is not None and dist.rank == 0:

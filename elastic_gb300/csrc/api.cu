@@ -4,6 +4,7 @@
 #include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "elx_krylov.h"
@@ -25,9 +26,11 @@ struct elx_ctx {
 
   // mesh (colour order) and structure
   DBuf conn, mat, elnum, slot, x, eq, e;
-  DBuf ia, ja, iat, jat, pt;
+  DBuf ia, ja;
+  // tiled transposed index of the SpMV and its halo slots
+  DBuf tile_tgt, tile_out, tgt_col, tgt_start, tpos, halo_ptr, halo_slot, part;
   // matrix
-  DBuf ad, al, alt, ad32, al32, alt32;
+  DBuf ad, al, ad32, al32;
   // state and solver vectors
   DBuf u, b0, b, xs, r, p, q, m, z;
   // scalars, partials, counters, flags
@@ -90,10 +93,18 @@ struct elx_ctx {
     elx::CsrcDev k;
     k.neq = s.neq; k.nad = s.nad;
     k.ia = ia.as<int32_t>(); k.ja = ja.as<int32_t>();
-    k.iat = iat.as<int32_t>(); k.jat = jat.as<int32_t>(); k.pt = pt.as<int32_t>();
-    k.ad = ad.as<double>(); k.al = al.as<double>(); k.alt = alt.as<double>();
-    k.ad32 = ad32.as<float>(); k.al32 = al32.as<float>(); k.alt32 = alt32.as<float>();
+    k.ad = ad.as<double>(); k.al = al.as<double>();
+    k.ad32 = ad32.as<float>(); k.al32 = al32.as<float>();
     return k;
+  }
+  elx::TileDev tile_dev() const {
+    elx::TileDev t;
+    t.rows = s.tile_rows; t.ntiles = s.ntiles; t.max_nnz = s.max_tile_nnz; t.lanes = s.lanes;
+    t.tile_tgt = tile_tgt.as<int32_t>(); t.tile_out = tile_out.as<int32_t>();
+    t.tgt_col = tgt_col.as<int32_t>(); t.tgt_start = tgt_start.as<int32_t>();
+    t.halo_ptr = halo_ptr.as<int32_t>(); t.halo_slot = halo_slot.as<int32_t>();
+    t.tpos = tpos.as<uint16_t>();
+    return t;
   }
 };
 
@@ -118,6 +129,22 @@ int guarded(elx_ctx *ctx, F &&f) {
 
 void require(bool c, int code, const char *what) {
   if (!c) throw Error{code, what};
+}
+
+// Rows per SpMV tile: the largest of 128/64/32 whose FP64 tile (11 bytes of
+// shared memory per entry) lets three CTAs share an SM; ELX_TILE_ROWS
+// overrides (tuning).
+int tile_rows_for(const elx::Structure &s) {
+  if (const char *env = getenv("ELX_TILE_ROWS")) {
+    const int r = atoi(env);
+    if (r >= 16 && r <= 256) return r;
+  }
+  const double mean = s.neq ? (double)s.nad / s.neq : 0.0;
+  for (int r : {128, 64}) {
+    const double bytes = 1.3 * mean * r * 11 + 16.0 * r;
+    if (bytes <= 72 * 1024) return r;
+  }
+  return 32;
 }
 
 // Uploads everything the kernels need once the structure is known.
@@ -151,16 +178,21 @@ void upload_structure(elx_ctx *c) {
   c->upload(c->e, m.e.data(), m.e.size());
   c->upload(c->ia, ia0.data(), ia0.size());
   c->upload(c->ja, ja0.data(), ja0.size());
-  c->upload(c->iat, s.iat.data(), s.iat.size());
-  c->upload(c->jat, s.jat.data(), s.jat.size());
-  c->upload(c->pt, s.pt.data(), s.pt.size());
+  elx::build_tiles(s, tile_rows_for(s));
+  c->upload(c->tile_tgt, s.tile_tgt.data(), s.tile_tgt.size());
+  c->upload(c->tile_out, s.tile_out.data(), s.tile_out.size());
+  c->upload(c->tgt_col, s.tgt_col.data(), s.tgt_col.size());
+  c->upload(c->tgt_start, s.tgt_start.data(), s.tgt_start.size());
+  c->upload(c->tpos, s.tpos.data(), s.tpos.size());
+  c->upload(c->halo_ptr, s.halo_ptr.data(), s.halo_ptr.size());
+  c->upload(c->halo_slot, s.halo_slot.data(), s.halo_slot.size());
+  c->alloc(c->part, (size_t)s.tile_out[s.ntiles] * 8);
+  elx::prepare_tile_kernels(c->tile_dev());
   const size_t n = (size_t)s.neq, nad = (size_t)s.nad;
   c->alloc(c->ad, n * 8);
   c->alloc(c->al, nad * 8);
-  c->alloc(c->alt, nad * 8);
   c->release(c->ad32);
   c->release(c->al32);
-  c->release(c->alt32);
   c->have_fp32 = false;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
@@ -186,7 +218,6 @@ void upload_structure(elx_ctx *c) {
   if (!c->ad32.p) {
     c->alloc(c->ad32, n * 4);
     c->alloc(c->al32, nad * 4);
-    c->alloc(c->alt32, nad * 4);
   }
   elx::launch_demote_values(c->csrc_dev(), c->stream);
   c->have_fp32 = true;
@@ -206,8 +237,7 @@ void assemble_resident(elx_ctx *c) {
   const elx::CsrcDev k = c->csrc_dev();
   for (const elx::Segment &seg : s.segments)
     elx::launch_assembly(md, k, seg, c->u.as<double>(), c->b.as<double>(), bad, c->stream);
-  elx::launch_transpose_values(k, c->stream);
-  c->launches += (int64_t)s.segments.size() + (s.nad ? 1 : 0);
+  c->launches += (int64_t)s.segments.size();
   ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   c->sync();
   c->have_fp32 = false;
@@ -243,9 +273,10 @@ void capture_pcg_graph(elx_ctx *c) {
   ELX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   const elx::CsrcDev k = c->csrc_dev();
   try {
+    const elx::TileDev td = c->tile_dev();
     for (int i = 0; i < kBatch; i++)
-      elx::launch_pcg_iteration(k, c->xs.as<double>(), c->r.as<double>(), c->p.as<double>(),
-                                c->q.as<double>(), c->m.as<double>(),
+      elx::launch_pcg_iteration(k, td, c->xs.as<double>(), c->r.as<double>(), c->p.as<double>(),
+                                c->q.as<double>(), c->part.as<double>(), c->m.as<double>(),
                                 c->scal.as<elx::PcgScalars>(), c->partials.as<double>(),
                                 c->counters.as<unsigned int>(), c->stream);
   } catch (...) {
@@ -277,12 +308,10 @@ void fill_info(elx_ctx *c, elx_info *info, const elx::PcgScalars &sc, double sec
   info->inner_iters = 0;
 }
 
-// y = K x for resident vectors (FP64), with the PCG's own SpMV kernel; the
-// dot product it also forms goes to scalar slot 1 (never marked done).
+// y = K x for resident vectors (FP64), with the PCG's own SpMV launches.
 void spmv64(elx_ctx *c, const double *x, double *y) {
-  elx::launch_spmv_dot(c->csrc_dev(), x, y, c->scal.as<elx::PcgScalars>() + 1,
-                       c->partials.as<double>(), c->counters.as<unsigned int>() + 4, c->stream);
-  c->launches += 1;
+  elx::launch_spmv64(c->csrc_dev(), c->tile_dev(), x, y, c->part.as<double>(), c->stream);
+  c->launches += 2;
 }
 
 void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
@@ -303,7 +332,7 @@ void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
   int launched = 0, checked = 0;
   auto launch_batch = [&](int slot) {
     ELX_CUDA(cudaGraphLaunch(c->pcg_graph, c->stream));
-    c->launches += 3 * c->pcg_graph_iters;
+    c->launches += 4 * c->pcg_graph_iters;
     ELX_CUDA(cudaMemcpyAsync(&c->h_scal[slot], d_sc, sizeof(elx::PcgScalars),
                              cudaMemcpyDeviceToHost, c->stream));
     ELX_CUDA(cudaEventRecord(c->ev[slot], c->stream));
@@ -456,8 +485,9 @@ void elx_destroy(elx_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->drop_graphs();
   for (DBuf *d : {&c->conn, &c->mat, &c->elnum, &c->slot, &c->x, &c->eq, &c->e, &c->ia, &c->ja,
-                  &c->iat, &c->jat, &c->pt, &c->ad, &c->al, &c->alt, &c->ad32, &c->al32,
-                  &c->alt32, &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
+                  &c->tile_tgt, &c->tile_out, &c->tgt_col, &c->tgt_start, &c->tpos,
+                  &c->halo_ptr, &c->halo_slot, &c->part, &c->ad, &c->al, &c->ad32, &c->al32,
+                  &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
                   &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
     c->release(*d);
   for (auto &e : c->ev)
@@ -647,8 +677,6 @@ int elx_set_matrix(elx_ctx *c, const double *ad, const double *al) {
     if (c->s.nad)
       ELX_CUDA(cudaMemcpyAsync(c->al.p, al, (size_t)c->s.nad * 8, cudaMemcpyHostToDevice,
                                c->stream));
-    elx::launch_transpose_values(c->csrc_dev(), c->stream);
-    c->launches += 1;
     c->sync();
     c->have_matrix = true;
     c->have_fp32 = false;

@@ -75,13 +75,25 @@ struct Structure {
   std::vector<int32_t> ia;    // (neq+1) 1-based
   std::vector<int32_t> ja;    // (nad)   1-based
   // derived, 0-based
-  std::vector<int32_t> iat, jat, pt;    // transposed index: CSR of the upper part
   std::vector<int32_t> elem_order;      // colour-ordered element list (0-based)
   std::vector<Segment> segments;        // per colour and element type
   std::vector<int32_t> color_of_segment;
   int32_t ncolors = 0;
   std::vector<int32_t> slot;            // (npairs, numel) in colour order
   int32_t npairs = 0;
+  // Tiled transposed index of the strict lower part (see spmv.cu): rows in
+  // tiles of tile_rows; per tile its distinct columns ("targets", ascending:
+  // first those left of the tile, then those inside), per target the tile-
+  // local positions of its entries, and per row the halo slots that the
+  // tiles to its right fill for it.
+  int32_t tile_rows = 0, ntiles = 0, max_tile_nnz = 0, lanes = 8;
+  std::vector<int32_t> tile_tgt;   // (ntiles+1) first target of each tile
+  std::vector<int32_t> tile_out;   // (ntiles+1) first halo slot of each tile
+  std::vector<int32_t> tgt_col;    // (ntargets) 0-based column
+  std::vector<int32_t> tgt_start;  // (ntargets+1) start of the target's positions in tpos
+  std::vector<uint16_t> tpos;      // (nad) tile-local entry positions, target order
+  std::vector<int32_t> halo_ptr;   // (neq+1)
+  std::vector<int32_t> halo_slot;  // (nhalo) slots, tile order within a row
 };
 
 // host structure routines (structure.cpp)
@@ -94,6 +106,7 @@ void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> 
                   const std::vector<int32_t> &adj, std::vector<int32_t> &ia,
                   std::vector<int32_t> &ja);
 void derive_structure(const Mesh &m, Structure &s);
+void build_tiles(Structure &s, int tile_rows);
 
 // ------------------------------------------------------------- kernels
 struct MeshDev {
@@ -113,21 +126,29 @@ struct CsrcDev {
   int64_t nad;
   const int32_t *ia;   // (neq+1) 0-based positions
   const int32_t *ja;   // (nad)   0-based columns
-  const int32_t *iat;  // (neq+1) upper part row pointers
-  const int32_t *jat;  // (nad)   upper part columns (= lower-part row)
-  const int32_t *pt;   // (nad)   position in al of each upper entry
-  double *ad, *al, *alt;
-  float *ad32, *al32, *alt32;
+  double *ad, *al;
+  float *ad32, *al32;
+};
+
+struct TileDev {
+  int32_t rows, ntiles, max_nnz, lanes;
+  const int32_t *tile_tgt, *tile_out, *tgt_col, *tgt_start, *halo_ptr, *halo_slot;
+  const uint16_t *tpos;
 };
 
 // assemble.cu
 void launch_assembly(const MeshDev &m, const CsrcDev &k, const Segment &seg,
                      const double *u, double *b, int32_t *bad_elem,
                      cudaStream_t st);
-// spmv.cu
-void launch_spmv64(const CsrcDev &k, const double *x, double *y, cudaStream_t st);
-void launch_spmv32(const CsrcDev &k, const float *x, float *y, cudaStream_t st);
-void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
+// spmv.cu: y = K x in two launches (tiles, then halo); the halo launch can
+// also form (p, y) and alpha for the PCG (sc != nullptr).
+struct PcgScalars;
+size_t tile_smem_bytes(const TileDev &t, bool fp32);
+void prepare_tile_kernels(const TileDev &t);
+void launch_tile_spmv64(const CsrcDev &k, const TileDev &t, const double *x, double *ytile,
+                        double *part, cudaStream_t st);
+void launch_tile_spmv32(const CsrcDev &k, const TileDev &t, const float *x, float *ytile,
+                        float *part, cudaStream_t st);
 void launch_demote_values(const CsrcDev &k, cudaStream_t st);
 
 }  // namespace elx

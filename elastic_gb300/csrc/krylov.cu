@@ -1,9 +1,10 @@
 // Jacobi-preconditioned CG on the GPU (pcg, mef/src/Iters.f:252-524, with
 // the diagonal preconditioner of Solv.f:65-69 / Precond.f:22-45).
 //
-// One iteration is three kernels that keep every scalar on the device, so the
+// One iteration is four kernels that keep every scalar on the device, so the
 // host never waits inside the loop:
-//   1. q = K p fused with the dot (p, q); the last block to finish computes
+//   1. q = K p: the tiled single-read SpMV (spmv.cu), then its halo launch
+//      fused with the dot (p, q); the last block to finish computes
 //      alpha = d / (p, q)                                   (Iters.f:366-372)
 //   2. x += alpha p, r -= alpha q, z = M r (not stored) fused with (r, z);
 //      the last block computes beta, d and the stopping test
@@ -20,8 +21,6 @@ namespace elx {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kLanes = 8;                       // threads per SpMV row
-constexpr int kRowsPerBlock = kThreads / kLanes;
 
 template <class T>
 __device__ __forceinline__ T warp_sum(T v) {
@@ -125,29 +124,23 @@ pcg_start_kernel(int n, const double *__restrict__ b, const double *__restrict__
   }
 }
 
-// q = K p and (p, q); alpha = d / (p, q).
+// Second launch of the SpMV (spmv.cu): y(i) = ytile(i) + its halo slots in
+// tile order, in place.  With sc != nullptr it also forms (p, y) and
+// alpha = d / (p, y) for the PCG (Iters.f:366-372).
 __global__ void __launch_bounds__(kThreads)
-pcg_spmv_dot_kernel(CsrcDev k, const double *__restrict__ p, double *__restrict__ q,
-                    PcgScalars *sc, double *partials, unsigned int *counter) {
-  if (sc->done) return;
-  const int lane = threadIdx.x % kLanes, sub = threadIdx.x / kLanes;
+halo_dot_kernel(int neq, const int32_t *__restrict__ halo_ptr,
+                const int32_t *__restrict__ halo_slot, const double *__restrict__ part,
+                const double *__restrict__ p, double *__restrict__ y, PcgScalars *sc,
+                double *partials, unsigned int *counter) {
+  if (sc && sc->done) return;
   double v[1] = {0.0};
-  for (int row0 = blockIdx.x * kRowsPerBlock; row0 < k.neq; row0 += gridDim.x * kRowsPerBlock) {
-    const int row = row0 + sub;
-    double s = 0.0;
-    if (row < k.neq) {
-      for (int j = k.ia[row] + lane; j < k.ia[row + 1]; j += kLanes) s += k.al[j] * p[k.ja[j]];
-      for (int j = k.iat[row] + lane; j < k.iat[row + 1]; j += kLanes) s += k.alt[j] * p[k.jat[j]];
-    }
-#pragma unroll
-    for (int off = kLanes / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, kLanes);
-    if (row < k.neq && lane == 0) {
-      const double pi = p[row];
-      const double qi = k.ad[row] * pi + s;
-      q[row] = qi;
-      v[0] += pi * qi;
-    }
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < neq; i += gridDim.x * kThreads) {
+    double yi = y[i];
+    for (int h = halo_ptr[i]; h < halo_ptr[i + 1]; h++) yi += part[halo_slot[h]];
+    y[i] = yi;
+    if (sc) v[0] += p[i] * yi;
   }
+  if (!sc) return;
   block_sum<1>(v);
   if (!publish_partials<1>(v, partials, counter)) return;
   double tot[1];
@@ -232,11 +225,6 @@ int vector_grid(int n) {
   return g < 1216 ? (g < 1 ? 1 : g) : 1216;
 }
 
-int spmv_grid(int neq) {
-  int g = (neq + kRowsPerBlock - 1) / kRowsPerBlock;
-  return g < 2432 ? (g < 1 ? 1 : g) : 2432;
-}
-
 void launch_diag_inverse(int n, const double *ad, double *m, int32_t *zero_row, cudaStream_t st) {
   diag_inverse_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, ad, m, zero_row);
   ELX_CUDA(cudaGetLastError());
@@ -248,22 +236,26 @@ void launch_pcg_start(int n, const double *b, const double *m, double *x, double
   ELX_CUDA(cudaGetLastError());
 }
 
-void launch_pcg_iteration(const CsrcDev &k, double *x, double *r, double *p, double *q,
-                          const double *m, PcgScalars *sc, double *partials,
-                          unsigned int *counters, cudaStream_t st) {
+void launch_pcg_iteration(const CsrcDev &k, const TileDev &td, double *x, double *r, double *p,
+                          double *q, double *part, const double *m, PcgScalars *sc,
+                          double *partials, unsigned int *counters, cudaStream_t st) {
   const int n = k.neq;
-  pcg_spmv_dot_kernel<<<spmv_grid(n), kThreads, 0, st>>>(k, p, q, sc, partials, counters + 0);
+  launch_tile_spmv64(k, td, p, q, part, st);
+  halo_dot_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, td.halo_ptr, td.halo_slot, part, p, q,
+                                                       sc, partials, counters + 0);
   pcg_update_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, p, q, m, x, r, sc, partials,
                                                          counters + 1);
   pcg_direction_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, r, m, p, sc);
   ELX_CUDA(cudaGetLastError());
 }
 
-// The PCG's fused SpMV as a standalone product y = K x (the dot it also
-// forms lands in the scalars at sc, which must have done == 0).
-void launch_spmv_dot(const CsrcDev &k, const double *x, double *y, PcgScalars *sc,
-                     double *partials, unsigned int *counter, cudaStream_t st) {
-  pcg_spmv_dot_kernel<<<spmv_grid(k.neq), kThreads, 0, st>>>(k, x, y, sc, partials, counter);
+// y = K x with the PCG's own two SpMV launches (no dot).
+void launch_spmv64(const CsrcDev &k, const TileDev &td, const double *x, double *y,
+                   double *part, cudaStream_t st) {
+  launch_tile_spmv64(k, td, x, y, part, st);
+  halo_dot_kernel<<<vector_grid(k.neq), kThreads, 0, st>>>(k.neq, td.halo_ptr, td.halo_slot,
+                                                            part, nullptr, y, nullptr, nullptr,
+                                                            nullptr);
   ELX_CUDA(cudaGetLastError());
 }
 

@@ -1,11 +1,12 @@
 // Host-side structure of the solve path: node graph, RCM permutation,
 // equation numbering and the lower CSRC pattern (all bit-identical to the
 // reference's), plus what the GPU kernels need beyond the reference's
-// arrays: the transposed index of the strict lower part, an element colouring
-// and the per-element slot map used by the assembly kernels.
+// arrays: the tiled transposed index of the SpMV, an element colouring and
+// the per-element slot map used by the assembly kernels.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <thread>
 
 #include "elx_internal.h"
 
@@ -266,34 +267,15 @@ void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> 
   }
 }
 
-// What the kernels need beyond ia/ja/id:
-//  * the transposed index: for every equation c the lower-part entries in
-//    column c (their rows jat and positions pt in al), ascending by row;
+// What the assembly kernels need beyond ia/ja/id:
 //  * a greedy element colouring in which no two elements of a colour share a
 //    node (so colour-ordered assembly needs no atomics), elements grouped per
 //    colour and element type;
 //  * the slot map: for each element and each unordered pair of its nodes
 //    {a, b} with free dofs, the offset within the row of the higher node of
 //    the lower node's first column (identical for every dof row of that node).
+// The SpMV's tiled transposed index is built by build_tiles.
 void derive_structure(const Mesh &m, Structure &s) {
-  const int32_t neq = s.neq;
-  const int64_t nad = s.nad;
-  // ---- transposed index (counting sort by column)
-  s.iat.assign(neq + 1, 0);
-  for (int64_t k = 0; k < nad; k++) s.iat[s.ja[k]]++;  // ja is 1-based: col c -> iat[c]
-  for (int c = 0; c < neq; c++) s.iat[c + 1] += s.iat[c];
-  s.jat.assign(nad, 0);
-  s.pt.assign(nad, 0);
-  {
-    std::vector<int32_t> fill(s.iat.begin(), s.iat.end() - 1);
-    for (int r = 0; r < neq; r++)
-      for (int32_t k = s.ia[r] - 1; k < s.ia[r + 1] - 1; k++) {
-        int c = s.ja[k] - 1;
-        int32_t q = fill[c]++;
-        s.jat[q] = r;
-        s.pt[q] = k;
-      }
-  }
   // ---- element colouring
   const int nen1 = m.nen + 1;
   std::vector<int32_t> color(m.numel, -1);
@@ -369,6 +351,125 @@ void derive_structure(const Mesh &m, Structure &s) {
         s.slot[(size_t)pair * m.numel + t] = (int32_t)(pos - rb);
       }
   }
+}
+
+namespace {
+
+template <class F>
+void parallel_for(int n, F &&f) {
+  int nt = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (n < 64) nt = 1;
+  std::vector<std::thread> th;
+  for (int w = 0; w < nt; w++)
+    th.emplace_back([&, w] {
+      for (int i = w; i < n; i += nt) f(i);
+    });
+  for (auto &t : th) t.join();
+}
+
+}  // namespace
+
+// Tiled transposed index for the single-read symmetric SpMV (spmv.cu).
+// Rows are cut into tiles of tile_rows consecutive rows.  For tile t its
+// entries are the CSRC positions [ia[r0], ia[r1]); every distinct column j
+// of those entries is a "target" that receives sum a_k x_row(k) over the
+// tile's entries in column j.  Targets are ascending by column, so the ones
+// left of the tile (j < r0, whose rows belong to earlier tiles) come first;
+// each of those gets a halo slot, and every row lists its halo slots in tile
+// order, which fixes the summation order of every y entry.
+void build_tiles(Structure &s, int tile_rows) {
+  const int32_t neq = s.neq;
+  s.tile_rows = tile_rows;
+  s.ntiles = (neq + tile_rows - 1) / tile_rows;
+  const int nt = s.ntiles;
+  // lanes per row from the mean row length
+  const double mean_len = neq ? (double)s.nad / neq : 0.0;
+  s.lanes = mean_len < 8 ? 1 : 2;  // threads per row in the SpMV row phase
+  std::vector<int32_t> ntgt(nt, 0), nout(nt, 0);
+  std::vector<std::vector<uint64_t>> keys(nt);
+  s.tpos.assign(s.nad, 0);
+  int32_t max_nnz = 0;
+  for (int t = 0; t < nt; t++) {
+    const int r0 = t * tile_rows, r1 = std::min(neq, r0 + tile_rows);
+    max_nnz = std::max(max_nnz, s.ia[r1] - s.ia[r0]);
+  }
+  ELX_REQUIRE(max_nnz <= 65535, ELX_ERR_ARG, "tile too large for 16-bit positions");
+  s.max_tile_nnz = max_nnz;
+  // per tile: sort (column, position) pairs; count targets
+  parallel_for(nt, [&](int t) {
+    const int r0 = t * tile_rows, r1 = std::min(neq, r0 + tile_rows);
+    const int64_t b0 = s.ia[r0] - 1, b1 = s.ia[r1] - 1;
+    std::vector<uint64_t> &kk = keys[t];
+    kk.resize(b1 - b0);
+    for (int64_t k = b0; k < b1; k++)
+      kk[k - b0] = ((uint64_t)(uint32_t)(s.ja[k] - 1) << 16) | (uint64_t)(k - b0);
+    std::sort(kk.begin(), kk.end());
+    int32_t c = 0, o = 0;
+    for (size_t q = 0; q < kk.size(); q++) {
+      const int32_t col = (int32_t)(kk[q] >> 16);
+      if (q == 0 || col != (int32_t)(kk[q - 1] >> 16)) {
+        c++;
+        if (col < r0) o++;
+      }
+    }
+    ntgt[t] = c;
+    nout[t] = o;
+  });
+  s.tile_tgt.assign(nt + 1, 0);
+  s.tile_out.assign(nt + 1, 0);
+  for (int t = 0; t < nt; t++) {
+    s.tile_tgt[t + 1] = s.tile_tgt[t] + ntgt[t];
+    s.tile_out[t + 1] = s.tile_out[t] + nout[t];
+  }
+  const int32_t ntargets = s.tile_tgt[nt];
+  s.tgt_col.assign(ntargets, 0);
+  s.tgt_start.assign(ntargets + 1, 0);
+  // Within each class (left of the tile, inside it) the targets are ordered
+  // by decreasing entry count, so that the 32 threads of a warp in the
+  // column phase run loops of nearly equal length (the FP64 pipe is charged
+  // per warp instruction, whatever the number of active lanes).
+  parallel_for(nt, [&](int t) {
+    const int r0 = t * tile_rows;
+    const int64_t b0 = s.ia[r0] - 1;
+    const std::vector<uint64_t> &kk = keys[t];
+    struct Run { int32_t col, begin, len; };
+    std::vector<Run> runs;
+    for (size_t q = 0; q < kk.size(); q++) {
+      const int32_t col = (int32_t)(kk[q] >> 16);
+      if (q == 0 || col != (int32_t)(kk[q - 1] >> 16)) runs.push_back({col, (int32_t)q, 0});
+      runs.back().len++;
+    }
+    const int32_t no = nout[t];
+    auto by_len = [](const Run &a, const Run &b) {
+      return a.len != b.len ? a.len > b.len : a.col < b.col;
+    };
+    std::stable_sort(runs.begin(), runs.begin() + no, by_len);
+    std::stable_sort(runs.begin() + no, runs.end(), by_len);
+    int32_t g = s.tile_tgt[t], q = 0;
+    for (const Run &r : runs) {
+      s.tgt_col[g] = r.col;
+      s.tgt_start[g] = (int32_t)(b0 + q);
+      for (int32_t e = 0; e < r.len; e++)
+        s.tpos[b0 + q + e] = (uint16_t)(kk[r.begin + e] & 0xffff);
+      q += r.len;
+      g++;
+    }
+  });
+  s.tgt_start[ntargets] = (int32_t)s.nad;
+  keys.clear();
+  keys.shrink_to_fit();
+  // halo lists per row, in tile order
+  s.halo_ptr.assign(neq + 1, 0);
+  for (int t = 0; t < nt; t++)
+    for (int32_t g = s.tile_tgt[t]; g < s.tile_tgt[t] + nout[t]; g++) s.halo_ptr[s.tgt_col[g] + 1]++;
+  for (int r = 0; r < neq; r++) s.halo_ptr[r + 1] += s.halo_ptr[r];
+  s.halo_slot.assign(s.halo_ptr[neq], 0);
+  std::vector<int32_t> fill(s.halo_ptr.begin(), s.halo_ptr.end() - 1);
+  for (int t = 0; t < nt; t++)
+    for (int32_t q = 0; q < nout[t]; q++) {
+      const int32_t g = s.tile_tgt[t] + q;
+      s.halo_slot[fill[s.tgt_col[g]]++] = s.tile_out[t] + q;
+    }
 }
 
 }  // namespace elx
