@@ -26,11 +26,12 @@ struct elx_ctx {
 
   // mesh (colour order) and structure
   DBuf conn, mat, elnum, slot, x, eq, e;
-  DBuf ia, ja;
+  DBuf ia, ja, iat, jat, pt;
   // tiled transposed index of the SpMV and its halo slots
-  DBuf tile_tgt, tile_out, tgt_col, tgt_start, tpos, halo_ptr, halo_slot, part;
+  DBuf tile_tgt, tile_out, tgt_col, tgt_start, tpos, halo_ptr, halo_slot, tile_desc, part;
   // matrix
-  DBuf ad, al, ad32, al32;
+  DBuf ad, al, alt, ad32, al32, alt32;
+  int spmv_kind = elx::kSpmvGather;  // FP64 SpMV kernel family
   // state and solver vectors
   DBuf u, b0, b, xs, r, p, q, m, z;
   // scalars, partials, counters, flags
@@ -68,9 +69,11 @@ struct elx_ctx {
     d.p = nullptr;
     d.bytes = 0;
   }
+  // Arrays read by bulk copies get 64 bytes of slack: a copy rounded out to
+  // 16-byte boundaries may read up to 15 bytes past the last element.
   template <class T>
   void upload(DBuf &d, const T *src, size_t n) {
-    alloc(d, n * sizeof(T));
+    alloc(d, n * sizeof(T) + 64);
     if (n) ELX_CUDA(cudaMemcpyAsync(d.p, src, n * sizeof(T), cudaMemcpyHostToDevice, stream));
   }
   void sync() { ELX_CUDA(cudaStreamSynchronize(stream)); }
@@ -93,13 +96,16 @@ struct elx_ctx {
     elx::CsrcDev k;
     k.neq = s.neq; k.nad = s.nad;
     k.ia = ia.as<int32_t>(); k.ja = ja.as<int32_t>();
-    k.ad = ad.as<double>(); k.al = al.as<double>();
-    k.ad32 = ad32.as<float>(); k.al32 = al32.as<float>();
+    k.iat = iat.as<int32_t>(); k.jat = jat.as<int32_t>(); k.pt = pt.as<int32_t>();
+    k.ad = ad.as<double>(); k.al = al.as<double>(); k.alt = alt.as<double>();
+    k.ad32 = ad32.as<float>(); k.al32 = al32.as<float>(); k.alt32 = alt32.as<float>();
     return k;
   }
   elx::TileDev tile_dev() const {
     elx::TileDev t;
-    t.rows = s.tile_rows; t.ntiles = s.ntiles; t.max_nnz = s.max_tile_nnz; t.lanes = s.lanes;
+    t.rows = s.tile_rows; t.ntiles = s.ntiles; t.max_nnz = s.max_tile_nnz;
+    t.max_tgt = s.max_tile_tgt; t.lanes = s.lanes;
+    t.desc = tile_desc.as<int32_t>();
     t.tile_tgt = tile_tgt.as<int32_t>(); t.tile_out = tile_out.as<int32_t>();
     t.tgt_col = tgt_col.as<int32_t>(); t.tgt_start = tgt_start.as<int32_t>();
     t.halo_ptr = halo_ptr.as<int32_t>(); t.halo_slot = halo_slot.as<int32_t>();
@@ -131,20 +137,28 @@ void require(bool c, int code, const char *what) {
   if (!c) throw Error{code, what};
 }
 
-// Rows per SpMV tile: the largest of 128/64/32 whose FP64 tile (11 bytes of
-// shared memory per entry) lets three CTAs share an SM; ELX_TILE_ROWS
-// overrides (tuning).
-int tile_rows_for(const elx::Structure &s) {
+// Rows per SpMV tile: the largest candidate whose three-stage FP64 pipeline
+// lets two CTAs share an SM's shared memory; ELX_TILE_ROWS overrides (tuning).
+void choose_tiles(elx::Structure &s) {
   if (const char *env = getenv("ELX_TILE_ROWS")) {
     const int r = atoi(env);
-    if (r >= 16 && r <= 256) return r;
+    if (r >= 8 && r <= 256) {
+      elx::build_tiles(s, r);
+      ELX_REQUIRE(elx::pipe_smem_bytes(s.max_tile_nnz, s.max_tile_tgt, r, false) <= 113 * 1024,
+                  ELX_ERR_ARG, "ELX_TILE_ROWS too large for shared memory");
+      return;
+    }
   }
   const double mean = s.neq ? (double)s.nad / s.neq : 0.0;
-  for (int r : {128, 64}) {
-    const double bytes = 1.3 * mean * r * 11 + 16.0 * r;
-    if (bytes <= 72 * 1024) return r;
+  for (int r : {96, 80, 64, 56, 48, 40, 32, 28, 24, 20, 16, 12, 8}) {
+    // estimate first (cheap), then build and check the exact size
+    if (r > 8 && elx::pipe_smem_bytes((int)(1.1 * mean * r) + 16, (int)(0.5 * mean * r) + 16, r,
+                                      false) > 110 * 1024)
+      continue;
+    elx::build_tiles(s, r);
+    if (elx::pipe_smem_bytes(s.max_tile_nnz, s.max_tile_tgt, r, false) <= 110 * 1024) return;
   }
-  return 32;
+  throw Error{ELX_ERR_ARG, "rows too long for the SpMV tiles"};
 }
 
 // Uploads everything the kernels need once the structure is known.
@@ -178,7 +192,13 @@ void upload_structure(elx_ctx *c) {
   c->upload(c->e, m.e.data(), m.e.size());
   c->upload(c->ia, ia0.data(), ia0.size());
   c->upload(c->ja, ja0.data(), ja0.size());
-  elx::build_tiles(s, tile_rows_for(s));
+  choose_tiles(s);
+  elx::build_transpose(s);
+  c->upload(c->iat, s.iat.data(), s.iat.size());
+  c->upload(c->jat, s.jat.data(), s.jat.size());
+  c->upload(c->pt, s.pt.data(), s.pt.size());
+  if (const char *env = getenv("ELX_SPMV"))
+    c->spmv_kind = std::string(env) == "tile" ? elx::kSpmvTiled : elx::kSpmvGather;
   c->upload(c->tile_tgt, s.tile_tgt.data(), s.tile_tgt.size());
   c->upload(c->tile_out, s.tile_out.data(), s.tile_out.size());
   c->upload(c->tgt_col, s.tgt_col.data(), s.tgt_col.size());
@@ -186,13 +206,16 @@ void upload_structure(elx_ctx *c) {
   c->upload(c->tpos, s.tpos.data(), s.tpos.size());
   c->upload(c->halo_ptr, s.halo_ptr.data(), s.halo_ptr.size());
   c->upload(c->halo_slot, s.halo_slot.data(), s.halo_slot.size());
+  c->upload(c->tile_desc, s.tile_desc.data(), s.tile_desc.size());
   c->alloc(c->part, (size_t)s.tile_out[s.ntiles] * 8);
   elx::prepare_tile_kernels(c->tile_dev());
   const size_t n = (size_t)s.neq, nad = (size_t)s.nad;
-  c->alloc(c->ad, n * 8);
-  c->alloc(c->al, nad * 8);
+  c->alloc(c->ad, n * 8 + 64);
+  c->alloc(c->al, nad * 8 + 64);
+  c->alloc(c->alt, nad * 8 + 64);
   c->release(c->ad32);
   c->release(c->al32);
+  c->release(c->alt32);
   c->have_fp32 = false;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
@@ -206,6 +229,7 @@ void upload_structure(elx_ctx *c) {
   c->alloc(c->counters, sizeof(unsigned int) * 16);
   ELX_CUDA(cudaMemsetAsync(c->counters.p, 0, c->counters.bytes, c->stream));
   c->alloc(c->flags, sizeof(int32_t) * 4);
+  ELX_CUDA(cudaMemsetAsync(c->flags.p, 0, c->flags.bytes, c->stream));
   c->alloc(c->diag, sizeof(double) * 8);
   c->sync();
   c->have_structure = true;
@@ -216,8 +240,9 @@ void upload_structure(elx_ctx *c) {
   if (c->have_fp32) return;
   const size_t n = (size_t)c->s.neq, nad = (size_t)c->s.nad;
   if (!c->ad32.p) {
-    c->alloc(c->ad32, n * 4);
-    c->alloc(c->al32, nad * 4);
+    c->alloc(c->ad32, n * 4 + 64);
+    c->alloc(c->al32, nad * 4 + 64);
+    c->alloc(c->alt32, nad * 4 + 64);
   }
   elx::launch_demote_values(c->csrc_dev(), c->stream);
   c->have_fp32 = true;
@@ -237,7 +262,8 @@ void assemble_resident(elx_ctx *c) {
   const elx::CsrcDev k = c->csrc_dev();
   for (const elx::Segment &seg : s.segments)
     elx::launch_assembly(md, k, seg, c->u.as<double>(), c->b.as<double>(), bad, c->stream);
-  c->launches += (int64_t)s.segments.size();
+  elx::launch_transpose_values(k, c->stream);
+  c->launches += (int64_t)s.segments.size() + (s.nad ? 1 : 0);
   ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   c->sync();
   c->have_fp32 = false;
@@ -275,10 +301,12 @@ void capture_pcg_graph(elx_ctx *c) {
   try {
     const elx::TileDev td = c->tile_dev();
     for (int i = 0; i < kBatch; i++)
-      elx::launch_pcg_iteration(k, td, c->xs.as<double>(), c->r.as<double>(), c->p.as<double>(),
+      elx::launch_pcg_iteration(k, td, c->spmv_kind, c->xs.as<double>(), c->r.as<double>(),
+                                c->p.as<double>(),
                                 c->q.as<double>(), c->part.as<double>(), c->m.as<double>(),
                                 c->scal.as<elx::PcgScalars>(), c->partials.as<double>(),
-                                c->counters.as<unsigned int>(), c->stream);
+                                c->counters.as<unsigned int>(), c->flags.as<int32_t>() + 2,
+                                c->stream);
   } catch (...) {
     cudaStreamEndCapture(c->stream, &g);
     throw;
@@ -310,8 +338,9 @@ void fill_info(elx_ctx *c, elx_info *info, const elx::PcgScalars &sc, double sec
 
 // y = K x for resident vectors (FP64), with the PCG's own SpMV launches.
 void spmv64(elx_ctx *c, const double *x, double *y) {
-  elx::launch_spmv64(c->csrc_dev(), c->tile_dev(), x, y, c->part.as<double>(), c->stream);
-  c->launches += 2;
+  elx::launch_spmv64(c->csrc_dev(), c->tile_dev(), c->spmv_kind, x, y, c->part.as<double>(),
+                     c->flags.as<int32_t>() + 2, c->stream);
+  c->launches += c->spmv_kind == elx::kSpmvTiled ? 2 : 1;
 }
 
 void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
@@ -332,7 +361,7 @@ void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
   int launched = 0, checked = 0;
   auto launch_batch = [&](int slot) {
     ELX_CUDA(cudaGraphLaunch(c->pcg_graph, c->stream));
-    c->launches += 4 * c->pcg_graph_iters;
+    c->launches += (c->spmv_kind == elx::kSpmvTiled ? 4 : 3) * c->pcg_graph_iters;
     ELX_CUDA(cudaMemcpyAsync(&c->h_scal[slot], d_sc, sizeof(elx::PcgScalars),
                              cudaMemcpyDeviceToHost, c->stream));
     ELX_CUDA(cudaEventRecord(c->ev[slot], c->stream));
@@ -485,8 +514,9 @@ void elx_destroy(elx_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->drop_graphs();
   for (DBuf *d : {&c->conn, &c->mat, &c->elnum, &c->slot, &c->x, &c->eq, &c->e, &c->ia, &c->ja,
-                  &c->tile_tgt, &c->tile_out, &c->tgt_col, &c->tgt_start, &c->tpos,
-                  &c->halo_ptr, &c->halo_slot, &c->part, &c->ad, &c->al, &c->ad32, &c->al32,
+                  &c->iat, &c->jat, &c->pt, &c->alt, &c->alt32, &c->tile_tgt, &c->tile_out, &c->tgt_col, &c->tgt_start, &c->tpos,
+                  &c->halo_ptr, &c->halo_slot, &c->tile_desc, &c->part, &c->ad, &c->al,
+                  &c->ad32, &c->al32,
                   &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
                   &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
     c->release(*d);
@@ -677,6 +707,8 @@ int elx_set_matrix(elx_ctx *c, const double *ad, const double *al) {
     if (c->s.nad)
       ELX_CUDA(cudaMemcpyAsync(c->al.p, al, (size_t)c->s.nad * 8, cudaMemcpyHostToDevice,
                                c->stream));
+    elx::launch_transpose_values(c->csrc_dev(), c->stream);
+    c->launches += c->s.nad ? 1 : 0;
     c->sync();
     c->have_matrix = true;
     c->have_fp32 = false;

@@ -86,7 +86,8 @@ struct Structure {
   // first those left of the tile, then those inside), per target the tile-
   // local positions of its entries, and per row the halo slots that the
   // tiles to its right fill for it.
-  int32_t tile_rows = 0, ntiles = 0, max_tile_nnz = 0, lanes = 8;
+  int32_t tile_rows = 0, ntiles = 0, max_tile_nnz = 0, max_tile_tgt = 0, lanes = 8;
+  std::vector<int32_t> tile_desc;  // (8, ntiles): base, nnz, g0, ng, o0, nout, r0, nr
   std::vector<int32_t> tile_tgt;   // (ntiles+1) first target of each tile
   std::vector<int32_t> tile_out;   // (ntiles+1) first halo slot of each tile
   std::vector<int32_t> tgt_col;    // (ntargets) 0-based column
@@ -94,6 +95,10 @@ struct Structure {
   std::vector<uint16_t> tpos;      // (nad) tile-local entry positions, target order
   std::vector<int32_t> halo_ptr;   // (neq+1)
   std::vector<int32_t> halo_slot;  // (nhalo) slots, tile order within a row
+  // Global transposed index of the strict lower part (CSR of the upper
+  // part): for each row c the entries of column c of L, by ascending row:
+  // their rows jat and their positions pt in al.
+  std::vector<int32_t> iat, jat, pt;
 };
 
 // host structure routines (structure.cpp)
@@ -107,6 +112,7 @@ void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> 
                   std::vector<int32_t> &ja);
 void derive_structure(const Mesh &m, Structure &s);
 void build_tiles(Structure &s, int tile_rows);
+void build_transpose(Structure &s);
 
 // ------------------------------------------------------------- kernels
 struct MeshDev {
@@ -126,13 +132,17 @@ struct CsrcDev {
   int64_t nad;
   const int32_t *ia;   // (neq+1) 0-based positions
   const int32_t *ja;   // (nad)   0-based columns
-  double *ad, *al;
-  float *ad32, *al32;
+  const int32_t *iat;  // (neq+1) upper part (transposed index) row pointers
+  const int32_t *jat;  // (nad)   upper part columns
+  const int32_t *pt;   // (nad)   position in al of each upper entry
+  double *ad, *al, *alt;
+  float *ad32, *al32, *alt32;
 };
 
 struct TileDev {
-  int32_t rows, ntiles, max_nnz, lanes;
+  int32_t rows, ntiles, max_nnz, max_tgt, lanes;
   const int32_t *tile_tgt, *tile_out, *tgt_col, *tgt_start, *halo_ptr, *halo_slot;
+  const int32_t *desc;  // (8, ntiles)
   const uint16_t *tpos;
 };
 
@@ -144,11 +154,19 @@ void launch_assembly(const MeshDev &m, const CsrcDev &k, const Segment &seg,
 // also form (p, y) and alpha for the PCG (sc != nullptr).
 struct PcgScalars;
 size_t tile_smem_bytes(const TileDev &t, bool fp32);
+size_t pipe_smem_bytes(int max_nnz, int max_tgt, int rows, bool fp32);
 void prepare_tile_kernels(const TileDev &t);
 void launch_tile_spmv64(const CsrcDev &k, const TileDev &t, const double *x, double *ytile,
-                        double *part, cudaStream_t st);
+                        double *part, int32_t *err, cudaStream_t st);
 void launch_tile_spmv32(const CsrcDev &k, const TileDev &t, const float *x, float *ytile,
-                        float *part, cudaStream_t st);
+                        float *part, int32_t *err, cudaStream_t st);
 void launch_demote_values(const CsrcDev &k, cudaStream_t st);
+void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
+// Two-sided gather SpMV: y = K x reading the lower part (ja, al) and the
+// upper part through the transposed copy (jat, alt); with sc != nullptr it
+// also forms (x, y) and alpha = d / (x, y).
+void launch_gather_spmv64(const CsrcDev &k, const double *x, double *y, PcgScalars *sc,
+                          double *partials, unsigned int *counter, cudaStream_t st);
+void launch_gather_spmv32(const CsrcDev &k, const float *x, float *y, cudaStream_t st);
 
 }  // namespace elx

@@ -3,7 +3,7 @@
 //
 // One iteration is four kernels that keep every scalar on the device, so the
 // host never waits inside the loop:
-//   1. q = K p: the tiled single-read SpMV (spmv.cu), then its halo launch
+//   1. q = K p: the pipelined single-read SpMV (spmv.cu), then its halo launch
 //      fused with the dot (p, q); the last block to finish computes
 //      alpha = d / (p, q)                                   (Iters.f:366-372)
 //   2. x += alpha p, r -= alpha q, z = M r (not stored) fused with (r, z);
@@ -16,72 +16,10 @@
 // block reduces its threads in a fixed tree and the last block to arrive
 // sums the block partials in a fixed order, so results are deterministic.
 #include "elx_krylov.h"
+#include "elx_reduce.cuh"
 
 namespace elx {
 namespace {
-
-constexpr int kThreads = 256;
-
-template <class T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-  return v;
-}
-
-// Block-wide sum of NV values (fixed order); result valid in thread 0.
-template <int NV>
-__device__ __forceinline__ void block_sum(double (&v)[NV]) {
-  __shared__ double sh[NV][kThreads / 32];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int i = 0; i < NV; i++) {
-    v[i] = warp_sum(v[i]);
-    if (lane == 0) sh[i][w] = v[i];
-  }
-  __syncthreads();
-  if (w == 0) {
-#pragma unroll
-    for (int i = 0; i < NV; i++) {
-      double t = lane < kThreads / 32 ? sh[i][lane] : 0.0;
-      v[i] = warp_sum(t);
-    }
-  }
-}
-
-// Writes this block's NV partials and returns true in thread 0 of the last
-// block to arrive, after which that thread may read every block's partials.
-template <int NV>
-__device__ __forceinline__ bool publish_partials(const double (&v)[NV], double *partials,
-                                                 unsigned int *counter) {
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int i = 0; i < NV; i++) partials[(size_t)i * gridDim.x + blockIdx.x] = v[i];
-    __threadfence();
-    const unsigned int ticket = atomicAdd(counter, 1u);
-    last = ticket == gridDim.x - 1;
-  }
-  __syncthreads();
-  return last;
-}
-
-// In the last block: every thread sums a strided slice of the partials, then
-// a fixed tree; thread 0 gets the totals and resets the counter.
-template <int NV>
-__device__ __forceinline__ void gather_partials(double (&tot)[NV], const double *partials,
-                                                unsigned int *counter) {
-  __threadfence();
-#pragma unroll
-  for (int i = 0; i < NV; i++) {
-    double s = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads)
-      s += ((volatile const double *)partials)[(size_t)i * gridDim.x + b];
-    tot[i] = s;
-  }
-  block_sum<NV>(tot);
-  if (threadIdx.x == 0) *counter = 0u;
-}
 
 // ------------------------------------------------------------ kernels
 __global__ void __launch_bounds__(kThreads)
@@ -236,13 +174,18 @@ void launch_pcg_start(int n, const double *b, const double *m, double *x, double
   ELX_CUDA(cudaGetLastError());
 }
 
-void launch_pcg_iteration(const CsrcDev &k, const TileDev &td, double *x, double *r, double *p,
-                          double *q, double *part, const double *m, PcgScalars *sc,
-                          double *partials, unsigned int *counters, cudaStream_t st) {
+void launch_pcg_iteration(const CsrcDev &k, const TileDev &td, int spmv_kind, double *x,
+                          double *r, double *p, double *q, double *part, const double *m,
+                          PcgScalars *sc, double *partials, unsigned int *counters,
+                          int32_t *err, cudaStream_t st) {
   const int n = k.neq;
-  launch_tile_spmv64(k, td, p, q, part, st);
-  halo_dot_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, td.halo_ptr, td.halo_slot, part, p, q,
-                                                       sc, partials, counters + 0);
+  if (spmv_kind == kSpmvTiled) {
+    launch_tile_spmv64(k, td, p, q, part, err, st);
+    halo_dot_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, td.halo_ptr, td.halo_slot, part, p,
+                                                         q, sc, partials, counters + 0);
+  } else {
+    launch_gather_spmv64(k, p, q, sc, partials, counters + 0, st);
+  }
   pcg_update_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, p, q, m, x, r, sc, partials,
                                                          counters + 1);
   pcg_direction_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, r, m, p, sc);
@@ -250,12 +193,16 @@ void launch_pcg_iteration(const CsrcDev &k, const TileDev &td, double *x, double
 }
 
 // y = K x with the PCG's own two SpMV launches (no dot).
-void launch_spmv64(const CsrcDev &k, const TileDev &td, const double *x, double *y,
-                   double *part, cudaStream_t st) {
-  launch_tile_spmv64(k, td, x, y, part, st);
-  halo_dot_kernel<<<vector_grid(k.neq), kThreads, 0, st>>>(k.neq, td.halo_ptr, td.halo_slot,
-                                                            part, nullptr, y, nullptr, nullptr,
-                                                            nullptr);
+void launch_spmv64(const CsrcDev &k, const TileDev &td, int spmv_kind, const double *x, double *y,
+                   double *part, int32_t *err, cudaStream_t st) {
+  if (spmv_kind == kSpmvTiled) {
+    launch_tile_spmv64(k, td, x, y, part, err, st);
+    halo_dot_kernel<<<vector_grid(k.neq), kThreads, 0, st>>>(k.neq, td.halo_ptr, td.halo_slot,
+                                                              part, nullptr, y, nullptr, nullptr,
+                                                              nullptr);
+  } else {
+    launch_gather_spmv64(k, x, y, nullptr, nullptr, nullptr, st);
+  }
   ELX_CUDA(cudaGetLastError());
 }
 

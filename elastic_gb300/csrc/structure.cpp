@@ -456,6 +456,21 @@ void build_tiles(Structure &s, int tile_rows) {
     }
   });
   s.tgt_start[ntargets] = (int32_t)s.nad;
+  s.tile_desc.assign((size_t)8 * nt, 0);
+  s.max_tile_tgt = 0;
+  for (int t = 0; t < nt; t++) {
+    const int r0 = t * tile_rows, r1 = std::min(neq, r0 + tile_rows);
+    int32_t *d = &s.tile_desc[(size_t)8 * t];
+    d[0] = s.ia[r0] - 1;
+    d[1] = s.ia[r1] - s.ia[r0];
+    d[2] = s.tile_tgt[t];
+    d[3] = ntgt[t];
+    d[4] = s.tile_out[t];
+    d[5] = nout[t];
+    d[6] = r0;
+    d[7] = r1 - r0;
+    s.max_tile_tgt = std::max(s.max_tile_tgt, ntgt[t]);
+  }
   keys.clear();
   keys.shrink_to_fit();
   // halo lists per row, in tile order
@@ -469,6 +484,26 @@ void build_tiles(Structure &s, int tile_rows) {
     for (int32_t q = 0; q < nout[t]; q++) {
       const int32_t g = s.tile_tgt[t] + q;
       s.halo_slot[fill[s.tgt_col[g]]++] = s.tile_out[t] + q;
+    }
+}
+
+// Transposed index of the strict lower part by a counting sort on columns:
+// iat/jat is the CSR of the upper part, pt the position in al of each of its
+// entries (so that alt = al[pt] is the upper part's value array).
+void build_transpose(Structure &s) {
+  const int32_t neq = s.neq;
+  s.iat.assign(neq + 1, 0);
+  for (int64_t k = 0; k < s.nad; k++) s.iat[s.ja[k]]++;  // 1-based column c counts at iat[c]
+  for (int c = 0; c < neq; c++) s.iat[c + 1] += s.iat[c];
+  s.jat.assign(s.nad, 0);
+  s.pt.assign(s.nad, 0);
+  std::vector<int32_t> fill(s.iat.begin(), s.iat.end() - 1);
+  for (int r = 0; r < neq; r++)
+    for (int32_t k = s.ia[r] - 1; k < s.ia[r + 1] - 1; k++) {
+      const int c = s.ja[k] - 1;
+      const int32_t q = fill[c]++;
+      s.jat[q] = r;
+      s.pt[q] = k;
     }
 }
 
