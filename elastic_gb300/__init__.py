@@ -113,6 +113,8 @@ def load():
         "elx_host_structure_get": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
         "elx_host_structure_destroy": (None, [_VP]),
         "elx_get_rhs": (C.c_int, [_VP, _F64]),
+        "elx_spmv_dot_noalloc": (C.c_int, [C.c_int32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                           _VP, _VP, _VP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -251,7 +251,9 @@ spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32
 // copy), UNROLL entries in flight per thread, then a fixed shuffle tree.
 // Rows are walked with a fixed grid so that the optional dot (x, y) reduces
 // in a fixed order.
-template <class T, int LANES, int U, bool DOT>
+// BASE is the index base of ia/ja/iat/jat contents (0 inside the library,
+// 1 for arrays in the reference's 1-based convention).
+template <class T, int LANES, int U, bool DOT, int BASE = 0>
 __global__ void __launch_bounds__(256)
 gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__restrict__ ja,
                    const T *__restrict__ al, const int32_t *__restrict__ iat,
@@ -270,7 +272,8 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
       for (int part = 0; part < 2; part++) {
         const int32_t *cols = part ? jat : ja;
         const T *vals = part ? alt : al;
-        const int kb = part ? iat[row] : ia[row], ke = part ? iat[row + 1] : ia[row + 1];
+        const int kb = (part ? iat[row] : ia[row]) - BASE;
+        const int ke = (part ? iat[row + 1] : ia[row + 1]) - BASE;
         for (int k0 = kb + lane; k0 < ke; k0 += U * LANES) {
           T a[U], xv[U];
           int j[U];
@@ -278,7 +281,7 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
           for (int u = 0; u < U; u++) {
             const int k = k0 + u * LANES;
             a[u] = k < ke ? vals[k] : T(0);
-            j[u] = k < ke ? cols[k] : row;
+            j[u] = k < ke ? cols[k] - BASE : row;
           }
 #pragma unroll
           for (int u = 0; u < U; u++) xv[u] = x[j[u]];
@@ -422,3 +425,68 @@ void launch_gather_spmv32(const CsrcDev &k, const float *x, float *y, cudaStream
 }
 
 }  // namespace elx
+
+// ---------------------------------------------------------------------------
+// Allocation-free entry point.
+//
+// Some callers cannot let a library allocate device memory: a driver that,
+// like the reference's own memory manager (one pool for everything), carves
+// all device arrays out of a pool it allocated once; code that runs where
+// cudaMalloc is not allowed or would synchronise the device in the middle of
+// an asynchronous pipeline.  elx_spmv_dot_noalloc serves them: the caller
+// passes every input and output as device pointers, and the only scratch the
+// kernel needs -- one partial sum per block, the last-block ticket and the
+// scalar slot of the fused dot product -- lives in the file-scope array
+// below, which every GPU that loads this library holds until the process
+// exits.
+namespace elx {
+namespace {
+
+constexpr int kNoAllocMaxBlocks = 16384;          // partial sums in the scratch
+constexpr int kNoAllocRowsPerBlock = 256 / 4;     // rows per block of the kernel
+constexpr int64_t kNoAllocMaxRows = (int64_t)kNoAllocMaxBlocks * kNoAllocRowsPerBlock;
+
+struct NoAllocScratch {
+  double partials[kNoAllocMaxBlocks];
+  PcgScalars scalars;
+  unsigned int counter;
+};
+
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Device address of the scratch per device, looked up once per device.
+constexpr int kMaxDevices = 64;
+NoAllocScratch *g_noalloc_addr[kMaxDevices] = {nullptr};
+
+}  // namespace
+}  // namespace elx
+
+extern "C" int elx_spmv_dot_noalloc(int32_t neq, const int32_t *ia, const int32_t *ja,
+                                    const double *ad, const double *al, const int32_t *iat,
+                                    const int32_t *jat, const double *alt, const double *x,
+                                    double *y, double *xy, void *stream) {
+  using namespace elx;
+  if (neq <= 0 || (int64_t)neq > kNoAllocMaxRows) return ELX_ERR_ARG;
+  if (!ia || !ja || !ad || !al || !iat || !jat || !alt || !x || !y || !xy) return ELX_ERR_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return ELX_ERR_CUDA;
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return ELX_ERR_CUDA;
+    g_noalloc_addr[dev] = static_cast<NoAllocScratch *>(p);
+  }
+  NoAllocScratch *sc = g_noalloc_addr[dev];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the ticket and the scalars must start at zero (done = 0 lets the kernel run)
+  if (cudaMemsetAsync(&sc->scalars, 0, sizeof(PcgScalars) + sizeof(unsigned int), st) !=
+      cudaSuccess)
+    return ELX_ERR_CUDA;
+  const int grid = (neq + kNoAllocRowsPerBlock - 1) / kNoAllocRowsPerBlock;
+  gather_spmv_kernel<double, 4, 4, true, 1><<<grid, 256, 0, st>>>(
+      neq, ia, ja, al, iat, jat, alt, ad, x, y, &sc->scalars, sc->partials, &sc->counter);
+  if (cudaGetLastError() != cudaSuccess) return ELX_ERR_CUDA;
+  if (cudaMemcpyAsync(xy, &sc->scalars.pq, sizeof(double), cudaMemcpyDeviceToDevice, st) !=
+      cudaSuccess)
+    return ELX_ERR_CUDA;
+  return ELX_OK;
+}

@@ -182,6 +182,34 @@ int elx_spmv_resident(elx_ctx *ctx, int32_t precision, int32_t reps);
 int elx_get_solution(elx_ctx *ctx, double *x);
 int elx_get_rhs(elx_ctx *ctx, double *b);
 
+/* ---- allocation-free SpMV + dot ---------------------------------------- */
+/* No counterpart in the reference: this entry point is for callers that
+ * cannot let the library allocate device memory -- a driver that, like the
+ * reference's own memory manager, keeps every device array in one pool it
+ * allocated up front, or code that must not call cudaMalloc because that
+ * would synchronise the device in the middle of its asynchronous work.  It
+ * needs no context: every input and output is a DEVICE pointer owned by the
+ * caller, and it computes y = K x (the CSRC product of matvec_csrcsym1) and
+ * *xy = (x, y), the product and dot of one PCG step, deterministically.
+ *   ia, ja, ad, al  the CSRC matrix, index contents 1-based as above;
+ *   iat, jat, alt   its upper part in CSR form, i.e. the transpose of the
+ *                   lower part (iat(neq+1) 1-based positions, jat(nad)
+ *                   1-based row numbers, alt(nad) the values of al in that
+ *                   order), e.g. from a counting sort of ja;
+ *   x (neq), y (neq), xy (1 double); stream: a cudaStream_t (NULL = default).
+ * Limit: neq <= 1048576 (ELX_ERR_ARG above; nothing is launched).  The
+ * scratch (one partial sum per 64 rows, a ticket and a scalar slot, about
+ * 130 KB) is a static device array that every GPU loading this library
+ * holds until the process exits.  The first call on a device looks up that
+ * array's device address (with the device current): make that first call
+ * before any stream capture.  All calls share the scratch, so calls that
+ * overlap on the GPU race; serialise them on one stream.  Returns ELX_OK
+ * once the work is enqueued on `stream`. */
+int elx_spmv_dot_noalloc(int32_t neq, const int32_t *ia, const int32_t *ja,
+                         const double *ad, const double *al, const int32_t *iat,
+                         const int32_t *jat, const double *alt, const double *x,
+                         double *y, double *xy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
