@@ -288,18 +288,19 @@ def run_spmv_only(args):
     except E.ElasticError:
         pass
     ext = torch.cuda.ExternalStream(ctx.stream, device=0)
-    ctx.spmv_resident(reps=args.warmup)
+    prec = E.PREC_MIXED if args.precision == "mixed" else E.PREC_FP64
+    ctx.spmv_resident(precision=prec, reps=args.warmup)
     torch.cuda.synchronize(0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(ext)
-    ctx.spmv_resident(reps=args.steps)
+    ctx.spmv_resident(precision=prec, reps=args.steps)
     e1.record(ext)
     torch.cuda.synchronize(0)
     ms = e0.elapsed_time(e1) / args.steps
-    byts = 12 * nad + 28 * neq
+    byts = 12 * nad + 28 * neq if prec == E.PREC_FP64 else 8 * nad + 16 * neq
     peak, kind = measured_peak()
     ctx.close()
-    return {"mode": "spmv", "neq": neq, "nad": nad, "spmv_ms": ms,
+    return {"mode": "spmv", "precision": args.precision, "neq": neq, "nad": nad, "spmv_ms": ms,
             "spmv_gbs": byts / (ms * 1e-3) / 1e9, "frac": byts / (ms * 1e-3) / 1e9 / peak,
             "peak": peak, "peak_kind": kind}
 
@@ -384,7 +385,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--mode", choices=["full", "spmv"], default="full",
-                    help="spmv: only the FP64 SpMV of the workload (for profiling)")
+                    help="spmv: only the SpMV of the workload (for profiling)")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
+                    help="solver precision (mixed: FP32 inner PCG + FP64 refinement)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     dist = Dist(args.impl)

@@ -34,6 +34,8 @@ struct elx_ctx {
   int spmv_kind = elx::kSpmvGather;  // FP64 SpMV kernel family
   // state and solver vectors
   DBuf u, b0, b, xs, r, p, q, m, z;
+  // mixed precision: FP32 inner PCG vectors and preconditioner
+  DBuf m32, p32, q32, r32, x32;
   // scalars, partials, counters, flags
   DBuf scal, partials, counters, flags, diag;
   elx::PcgScalars *h_scal = nullptr;  // pinned, 2 slots
@@ -42,7 +44,8 @@ struct elx_ctx {
 
   int64_t launches = 0;  // kernels of this library launched by this context
 
-  cudaGraphExec_t pcg_graph = nullptr;
+  cudaGraphExec_t pcg_graph = nullptr;    // kBatch FP64 PCG iterations
+  cudaGraphExec_t pcg32_graph = nullptr;  // kBatch FP32 inner PCG iterations
   int pcg_graph_iters = 0;
   cudaEvent_t ev[2] = {nullptr, nullptr};
 
@@ -79,7 +82,8 @@ struct elx_ctx {
   void sync() { ELX_CUDA(cudaStreamSynchronize(stream)); }
   void drop_graphs() {
     if (pcg_graph) cudaGraphExecDestroy(pcg_graph);
-    pcg_graph = nullptr;
+    if (pcg32_graph) cudaGraphExecDestroy(pcg32_graph);
+    pcg_graph = pcg32_graph = nullptr;
     pcg_graph_iters = 0;
   }
 
@@ -213,9 +217,8 @@ void upload_structure(elx_ctx *c) {
   c->alloc(c->ad, n * 8 + 64);
   c->alloc(c->al, nad * 8 + 64);
   c->alloc(c->alt, nad * 8 + 64);
-  c->release(c->ad32);
-  c->release(c->al32);
-  c->release(c->alt32);
+  for (DBuf *v : {&c->ad32, &c->al32, &c->alt32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32})
+    c->release(*v);
   c->have_fp32 = false;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
@@ -231,20 +234,26 @@ void upload_structure(elx_ctx *c) {
   c->alloc(c->flags, sizeof(int32_t) * 4);
   ELX_CUDA(cudaMemsetAsync(c->flags.p, 0, c->flags.bytes, c->stream));
   c->alloc(c->diag, sizeof(double) * 8);
+  c->drop_graphs();
   c->sync();
   c->have_structure = true;
   c->have_matrix = false;
 }
 
-[[maybe_unused]] void ensure_fp32(elx_ctx *c) {
-  if (c->have_fp32) return;
+// FP32 copies of the matrix (after each assembly) and the FP32 inner-solver
+// vectors (once per structure), allocated on first use.
+void ensure_fp32(elx_ctx *c) {
   const size_t n = (size_t)c->s.neq, nad = (size_t)c->s.nad;
   if (!c->ad32.p) {
     c->alloc(c->ad32, n * 4 + 64);
     c->alloc(c->al32, nad * 4 + 64);
     c->alloc(c->alt32, nad * 4 + 64);
+    for (DBuf *v : {&c->m32, &c->p32, &c->q32, &c->r32, &c->x32}) c->alloc(*v, n * 4 + 64);
+    c->drop_graphs();
   }
+  if (c->have_fp32) return;
   elx::launch_demote_values(c->csrc_dev(), c->stream);
+  c->launches += c->s.nad ? 2 : 1;
   c->have_fp32 = true;
 }
 
@@ -280,7 +289,8 @@ void build_preconditioner(elx_ctx *c) {
   const int32_t big = INT_MAX;
   int32_t *zero = c->flags.as<int32_t>() + 1;
   ELX_CUDA(cudaMemcpyAsync(zero, &big, sizeof(big), cudaMemcpyHostToDevice, c->stream));
-  elx::launch_diag_inverse(c->s.neq, c->ad.as<double>(), c->m.as<double>(), zero, c->stream);
+  elx::launch_diag_inverse(c->s.neq, c->ad.as<double>(), c->m.as<double>(),
+                           c->m32.p ? c->m32.as<float>() : nullptr, zero, c->stream);
   c->launches += 1;
   ELX_CUDA(cudaMemcpyAsync(c->h_flags + 1, zero, sizeof(int32_t), cudaMemcpyDeviceToHost,
                            c->stream));
@@ -292,30 +302,78 @@ void build_preconditioner(elx_ctx *c) {
 
 constexpr int kBatch = 16;  // PCG iterations per captured graph launch
 
-void capture_pcg_graph(elx_ctx *c) {
-  if (c->pcg_graph && c->pcg_graph_iters == kBatch) return;
-  c->drop_graphs();
+// Captures kBatch iterations (FP64 or the FP32 inner iteration) as a graph.
+cudaGraphExec_t capture_batch(elx_ctx *c, bool fp32) {
   cudaGraph_t g;
   ELX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   const elx::CsrcDev k = c->csrc_dev();
   try {
     const elx::TileDev td = c->tile_dev();
-    for (int i = 0; i < kBatch; i++)
-      elx::launch_pcg_iteration(k, td, c->spmv_kind, c->xs.as<double>(), c->r.as<double>(),
-                                c->p.as<double>(),
-                                c->q.as<double>(), c->part.as<double>(), c->m.as<double>(),
-                                c->scal.as<elx::PcgScalars>(), c->partials.as<double>(),
-                                c->counters.as<unsigned int>(), c->flags.as<int32_t>() + 2,
-                                c->stream);
+    for (int i = 0; i < kBatch; i++) {
+      if (fp32)
+        elx::launch_rel_iteration(k, c->b.as<double>(), c->m.as<double>(), c->xs.as<double>(),
+                                  c->r.as<double>(), c->z.as<double>(), c->x32.as<float>(),
+                                  c->r32.as<float>(), c->p32.as<float>(), c->q32.as<float>(),
+                                  c->m32.as<float>(), c->scal.as<elx::PcgScalars>(),
+                                  c->partials.as<double>(), c->counters.as<unsigned int>(),
+                                  c->stream);
+      else
+        elx::launch_pcg_iteration(k, td, c->spmv_kind, c->xs.as<double>(), c->r.as<double>(),
+                                  c->p.as<double>(), c->q.as<double>(), c->part.as<double>(),
+                                  c->m.as<double>(), c->scal.as<elx::PcgScalars>(),
+                                  c->partials.as<double>(), c->counters.as<unsigned int>(),
+                                  c->flags.as<int32_t>() + 2, c->stream);
+    }
   } catch (...) {
     cudaStreamEndCapture(c->stream, &g);
     throw;
   }
   ELX_CUDA(cudaStreamEndCapture(c->stream, &g));
-  const cudaError_t inst = cudaGraphInstantiate(&c->pcg_graph, g, 0);
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t inst = cudaGraphInstantiate(&exec, g, 0);
   cudaGraphDestroy(g);
   ELX_CUDA(inst);
+  return exec;
+}
+
+void capture_pcg_graph(elx_ctx *c) {
+  if (!c->pcg_graph) c->pcg_graph = capture_batch(c, false);
   c->pcg_graph_iters = kBatch;
+}
+
+// Launches batches of `graph` until the scalars' stopping flag is set (two
+// batches in flight; the host reads the flag of the older one).
+elx::PcgScalars run_batches(elx_ctx *c, cudaGraphExec_t graph, int kernels_per_iter,
+                            int maxit) {
+  elx::PcgScalars *d_sc = c->scal.as<elx::PcgScalars>();
+  int launched = 0, checked = 0;
+  auto launch_batch = [&](int slot) {
+    ELX_CUDA(cudaGraphLaunch(graph, c->stream));
+    c->launches += (int64_t)kernels_per_iter * kBatch;
+    ELX_CUDA(cudaMemcpyAsync(&c->h_scal[slot], d_sc, sizeof(elx::PcgScalars),
+                             cudaMemcpyDeviceToHost, c->stream));
+    ELX_CUDA(cudaEventRecord(c->ev[slot], c->stream));
+  };
+  const int max_batches = maxit / kBatch + 2;
+  launch_batch(0);
+  launched = 1;
+  if (max_batches > 1) {
+    launch_batch(1);
+    launched = 2;
+  }
+  for (;;) {
+    const int slot = checked & 1;
+    ELX_CUDA(cudaEventSynchronize(c->ev[slot]));
+    checked++;
+    if (c->h_scal[slot].done) break;
+    if (launched >= max_batches) break;  // guard; the kernels stop at maxit themselves
+    launch_batch(launched & 1);
+    launched++;
+  }
+  c->sync();
+  elx::PcgScalars last;
+  ELX_CUDA(cudaMemcpy(&last, d_sc, sizeof(last), cudaMemcpyDeviceToHost));
+  return last;
 }
 
 void fill_info(elx_ctx *c, elx_info *info, const elx::PcgScalars &sc, double secs) {
@@ -343,50 +401,9 @@ void spmv64(elx_ctx *c, const double *x, double *y) {
   c->launches += c->spmv_kind == elx::kSpmvTiled ? 2 : 1;
 }
 
-void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
-  auto t0 = std::chrono::steady_clock::now();
-  build_preconditioner(c);
-  elx::PcgScalars init{};
-  init.tol = tol;
-  init.maxit = maxit;
-  elx::PcgScalars *d_sc = c->scal.as<elx::PcgScalars>();
-  c->h_scal[0] = init;
-  ELX_CUDA(cudaMemcpyAsync(d_sc, &c->h_scal[0], sizeof(init), cudaMemcpyHostToDevice, c->stream));
-  elx::launch_pcg_start(c->s.neq, c->b.as<double>(), c->m.as<double>(), c->xs.as<double>(),
-                        c->r.as<double>(), c->p.as<double>(), d_sc, c->partials.as<double>(),
-                        c->counters.as<unsigned int>() + 2, c->stream);
-  c->launches += 1;
-  capture_pcg_graph(c);
-  // keep two batches in flight; read the stopping flag of the older one
-  int launched = 0, checked = 0;
-  auto launch_batch = [&](int slot) {
-    ELX_CUDA(cudaGraphLaunch(c->pcg_graph, c->stream));
-    c->launches += (c->spmv_kind == elx::kSpmvTiled ? 4 : 3) * c->pcg_graph_iters;
-    ELX_CUDA(cudaMemcpyAsync(&c->h_scal[slot], d_sc, sizeof(elx::PcgScalars),
-                             cudaMemcpyDeviceToHost, c->stream));
-    ELX_CUDA(cudaEventRecord(c->ev[slot], c->stream));
-  };
-  const int max_batches = maxit / kBatch + 2;
-  launch_batch(0);
-  launched = 1;
-  if (max_batches > 1) {
-    launch_batch(1);
-    launched = 2;
-  }
-  elx::PcgScalars last{};
-  for (;;) {
-    const int slot = checked & 1;
-    ELX_CUDA(cudaEventSynchronize(c->ev[slot]));
-    last = c->h_scal[slot];
-    checked++;
-    if (last.done) break;
-    if (launched >= max_batches) break;  // guard; the kernels stop at maxit themselves
-    launch_batch(launched & 1);
-    launched++;
-  }
-  c->sync();
-  ELX_CUDA(cudaMemcpy(&last, d_sc, sizeof(last), cudaMemcpyDeviceToHost));
-  // post-solve diagnostics (Iters.f:433-458)
+// Post-solve diagnostics (Iters.f:433-458) of the resident x: z = K x,
+// xKx, ||x||, ||b - Kx||_M, ||b - Kx|| into h_diag[0..3].
+void post_diagnostics(elx_ctx *c) {
   spmv64(c, c->xs.as<double>(), c->z.as<double>());
   elx::launch_diagnostics(c->s.neq, c->xs.as<double>(), c->z.as<double>(), c->b.as<double>(),
                           c->m.as<double>(), c->diag.as<double>(), c->partials.as<double>(),
@@ -395,6 +412,30 @@ void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
   ELX_CUDA(cudaMemcpyAsync(c->h_diag, c->diag.p, 4 * sizeof(double), cudaMemcpyDeviceToHost,
                            c->stream));
   c->sync();
+}
+
+void set_scalars(elx_ctx *c, double tol, int maxit) {
+  elx::PcgScalars init{};
+  init.tol = tol;
+  init.maxit = maxit;
+  c->h_scal[0] = init;
+  ELX_CUDA(cudaMemcpyAsync(c->scal.p, &c->h_scal[0], sizeof(init), cudaMemcpyHostToDevice,
+                           c->stream));
+}
+
+void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  build_preconditioner(c);
+  set_scalars(c, tol, maxit);
+  elx::launch_pcg_start<double>(c->s.neq, c->b.as<double>(), c->m.as<double>(),
+                                c->xs.as<double>(), c->r.as<double>(), c->p.as<double>(),
+                                c->scal.as<elx::PcgScalars>(), c->partials.as<double>(),
+                                c->counters.as<unsigned int>() + 2, c->stream);
+  c->launches += 1;
+  capture_pcg_graph(c);
+  elx::PcgScalars last =
+      run_batches(c, c->pcg_graph, c->spmv_kind == elx::kSpmvTiled ? 4 : 3, maxit);
+  post_diagnostics(c);
   const double secs =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (!last.done) last.status = ELX_ERR_NO_CONVERGENCE;
@@ -402,6 +443,59 @@ void pcg64(elx_ctx *c, double tol, int maxit, elx_info *info) {
   if (last.status != ELX_OK)
     throw Error{last.status, "no convergence after " + std::to_string(last.iters) +
                                  " iterations"};
+}
+
+// Mixed precision: FP32 CG with reliable updates (krylov.cu): the FP32
+// iteration carries the Krylov recurrence, the FP64 solution and the FP64
+// residual are refreshed each time the FP32 residual has dropped tenfold,
+// and the stopping test is the reference's, ||b - K x||_M < tol ||b||_M, on
+// the FP64 residual.
+void pcg_mixed(elx_ctx *c, double tol, int maxit, elx_info *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  ensure_fp32(c);
+  build_preconditioner(c);
+  if (!c->pcg32_graph) c->pcg32_graph = capture_batch(c, true);
+  const int n = c->s.neq;
+  double *bmb_d = c->diag.as<double>() + 4;
+  // r_hi = b (x = 0), r = (float) b, (b, M b) in FP64
+  elx::launch_refine_residual(n, c->b.as<double>(), nullptr, c->m.as<double>(),
+                              c->r.as<double>(), c->r32.as<float>(), bmb_d,
+                              c->partials.as<double>(), c->counters.as<unsigned int>() + 5,
+                              c->stream);
+  ELX_CUDA(cudaMemsetAsync(c->xs.p, 0, (size_t)n * 8, c->stream));
+  ELX_CUDA(cudaMemcpyAsync(c->h_diag + 4, bmb_d, sizeof(double), cudaMemcpyDeviceToHost,
+                           c->stream));
+  c->sync();
+  const double bmb = c->h_diag[4];
+  elx::PcgScalars init{};
+  init.tol = tol;
+  init.maxit = maxit;
+  init.bmb = bmb;
+  init.conv = tol * std::sqrt(std::fabs(bmb));
+  init.delta = 0.1;
+  c->h_scal[0] = init;
+  ELX_CUDA(cudaMemcpyAsync(c->scal.p, &c->h_scal[0], sizeof(init), cudaMemcpyHostToDevice,
+                           c->stream));
+  elx::launch_rel_start(n, c->r32.as<float>(), c->m32.as<float>(), c->x32.as<float>(),
+                        c->p32.as<float>(), c->scal.as<elx::PcgScalars>(),
+                        c->partials.as<double>(), c->counters.as<unsigned int>() + 2, c->stream);
+  c->launches += 2;
+  elx::PcgScalars last = run_batches(c, c->pcg32_graph, 6, maxit);
+  // fold the last FP32 piece (zero unless maxit stopped the iteration)
+  elx::launch_refine_accumulate(n, c->xs.as<double>(), c->x32.as<float>(), false, c->stream);
+  c->launches += 1;
+  post_diagnostics(c);
+  const double secs =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (!last.done) last.status = ELX_ERR_NO_CONVERGENCE;
+  fill_info(c, info, last, secs);
+  if (info) {
+    info->refinements = last.nupdates;
+    info->inner_iters = last.iters;
+  }
+  if (last.status != ELX_OK)
+    throw Error{last.status, "mixed precision: no convergence after " +
+                                 std::to_string(last.iters) + " iterations"};
 }
 
 void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit, int ngram,
@@ -412,6 +506,10 @@ void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit
   if (info) std::memset(info, 0, sizeof(*info));
   if (solver == ELX_SOLVER_PCG && precision == ELX_PREC_FP64) {
     pcg64(c, tol, maxit, info);
+    return;
+  }
+  if (solver == ELX_SOLVER_PCG && precision == ELX_PREC_MIXED) {
+    pcg_mixed(c, tol, maxit, info);
     return;
   }
   throw Error{ELX_ERR_ARG, "solver/precision combination not available"};
@@ -760,6 +858,14 @@ int elx_spmv(elx_ctx *c, int32_t precision, const double *x, double *y) {
     ELX_CUDA(cudaMemcpyAsync(c->p.p, x, n * 8, cudaMemcpyHostToDevice, c->stream));
     if (precision == ELX_PREC_FP64) {
       spmv64(c, c->p.as<double>(), c->q.as<double>());
+    } else if (precision == ELX_PREC_MIXED) {
+      // the FP32 product of the mixed-precision inner iteration
+      ensure_fp32(c);
+      elx::launch_convert((int)n, c->p.as<double>(), c->p32.as<float>(), c->stream);
+      elx::launch_gather_spmv32(c->csrc_dev(), c->p32.as<float>(), c->q32.as<float>(), nullptr,
+                                nullptr, nullptr, c->stream);
+      elx::launch_widen((int)n, c->q32.as<float>(), c->q.as<double>(), c->stream);
+      c->launches += 3;
     } else {
       throw Error{ELX_ERR_ARG, "precision not available"};
     }
@@ -771,8 +877,18 @@ int elx_spmv(elx_ctx *c, int32_t precision, const double *x, double *y) {
 int elx_spmv_resident(elx_ctx *c, int32_t precision, int32_t reps) {
   return guarded(c, [&] {
     require(c->have_matrix, ELX_ERR_STATE, "no matrix");
-    require(precision == ELX_PREC_FP64, ELX_ERR_ARG, "precision not available");
-    for (int i = 0; i < reps; i++) spmv64(c, c->p.as<double>(), c->q.as<double>());
+    if (precision == ELX_PREC_FP64) {
+      for (int i = 0; i < reps; i++) spmv64(c, c->p.as<double>(), c->q.as<double>());
+    } else if (precision == ELX_PREC_MIXED) {
+      ensure_fp32(c);
+      elx::launch_convert(c->s.neq, c->p.as<double>(), c->p32.as<float>(), c->stream);
+      for (int i = 0; i < reps; i++)
+        elx::launch_gather_spmv32(c->csrc_dev(), c->p32.as<float>(), c->q32.as<float>(),
+                                  nullptr, nullptr, nullptr, c->stream);
+      c->launches += 1 + reps;
+    } else {
+      throw Error{ELX_ERR_ARG, "precision not available"};
+    }
   });
 }
 

@@ -166,7 +166,9 @@ void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
 // upper part through the transposed copy (jat, alt); with sc != nullptr it
 // also forms (x, y) and alpha = d / (x, y).
 void launch_gather_spmv64(const CsrcDev &k, const double *x, double *y, PcgScalars *sc,
+                          double *partials, unsigned int *counter, cudaStream_t st,
+                          const int32_t *gate = nullptr);
+void launch_gather_spmv32(const CsrcDev &k, const float *x, float *y, PcgScalars *sc,
                           double *partials, unsigned int *counter, cudaStream_t st);
-void launch_gather_spmv32(const CsrcDev &k, const float *x, float *y, cudaStream_t st);
 
 }  // namespace elx

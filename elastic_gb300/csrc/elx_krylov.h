@@ -12,29 +12,50 @@ struct PcgScalars {
   double bmb;     // (b, M b)
   double conv;    // tol * sqrt|(b, M b)|
   double alpha, beta, pq;
+  double rmax;    // mixed precision: ||r||_M at the last residual replacement
+  double delta;   // mixed precision: replace when ||r||_M < delta * rmax (input)
   int32_t maxit;  // (input)
   int32_t iters;
   int32_t done;
   int32_t status;
+  int32_t update;    // mixed precision: a residual replacement is due
+  int32_t nupdates;  // mixed precision: replacements so far
 };
 
 int vector_grid(int n);
 
-void launch_diag_inverse(int n, const double *ad, double *m, int32_t *zero_row, cudaStream_t st);
-void launch_pcg_start(int n, const double *b, const double *m, double *x, double *r, double *p,
-                      PcgScalars *sc, double *partials, unsigned int *counter, cudaStream_t st);
 // SpMV kernel families (spmv.cu)
 constexpr int kSpmvGather = 0;  // two-sided gather (lower + transposed upper)
 constexpr int kSpmvTiled = 1;   // single-read tiles with a transposed index per tile
 
+void launch_diag_inverse(int n, const double *ad, double *m, float *m32, int32_t *zero_row,
+                         cudaStream_t st);
+template <class T>
+void launch_pcg_start(int n, const T *b, const T *m, T *x, T *r, T *p, PcgScalars *sc,
+                      double *partials, unsigned int *counter, cudaStream_t st);
 void launch_pcg_iteration(const CsrcDev &k, const TileDev &td, int spmv_kind, double *x,
                           double *r, double *p, double *q, double *part, const double *m,
                           PcgScalars *sc, double *partials, unsigned int *counters,
                           int32_t *err, cudaStream_t st);
+void launch_pcg_iteration32(const CsrcDev &k, float *x, float *r, float *p, float *q,
+                            const float *m, PcgScalars *sc, double *partials,
+                            unsigned int *counters, cudaStream_t st);
 void launch_spmv64(const CsrcDev &k, const TileDev &td, int spmv_kind, const double *x, double *y,
                    double *part, int32_t *err, cudaStream_t st);
 void launch_diagnostics(int n, const double *x, const double *z, const double *b,
                         const double *m, double *out, double *partials, unsigned int *counter,
                         cudaStream_t st);
+void launch_refine_residual(int n, const double *b, const double *z, const double *m, double *r,
+                            float *r32, double *out, double *partials, unsigned int *counter,
+                            cudaStream_t st);
+void launch_refine_accumulate(int n, double *x, const float *d, bool first, cudaStream_t st);
+void launch_rel_start(int n, const float *r, const float *m, float *xlo, float *p,
+                      PcgScalars *sc, double *partials, unsigned int *counter, cudaStream_t st);
+void launch_rel_iteration(const CsrcDev &k, const double *b, const double *m, double *xhi,
+                          double *rhi, double *z, float *xlo, float *r, float *p, float *q,
+                          const float *m32, PcgScalars *sc, double *partials,
+                          unsigned int *counters, cudaStream_t st);
+void launch_convert(int n, const double *src, float *dst, cudaStream_t st);
+void launch_widen(int n, const float *src, double *dst, cudaStream_t st);
 
 }  // namespace elx

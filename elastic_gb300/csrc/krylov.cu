@@ -1,20 +1,25 @@
 // Jacobi-preconditioned CG on the GPU (pcg, mef/src/Iters.f:252-524, with
-// the diagonal preconditioner of Solv.f:65-69 / Precond.f:22-45).
+// the diagonal preconditioner of Solv.f:65-69 / Precond.f:22-45), and its
+// mixed-precision form: FP32 inner PCG inside FP64 iterative refinement.
 //
-// One iteration is four kernels that keep every scalar on the device, so the
-// host never waits inside the loop:
-//   1. q = K p: the pipelined single-read SpMV (spmv.cu), then its halo launch
-//      fused with the dot (p, q); the last block to finish computes
-//      alpha = d / (p, q)                                   (Iters.f:366-372)
+// One PCG iteration is three kernels that keep every scalar on the device,
+// so the host never waits inside the loop:
+//   1. q = K p (spmv.cu) fused with the dot (p, q); the last block to finish
+//      computes alpha = d / (p, q)                            (Iters.f:366-372)
 //   2. x += alpha p, r -= alpha q, z = M r (not stored) fused with (r, z);
 //      the last block computes beta, d and the stopping test
-//      sqrt|d| < tol * ||b||_M                              (Iters.f:377-419)
-//   3. p = M r + beta p                                     (Iters.f:411-414)
+//      sqrt|d| < tol * ||b||_M                                (Iters.f:377-419)
+//   3. p = M r + beta p                                       (Iters.f:411-414)
 // Every kernel returns at once when the stopping flag is set, so the host can
 // enqueue iterations in batches (captured once as a CUDA graph) and read the
-// flag between batches.  Reductions are two-level with a fixed grid: each
-// block reduces its threads in a fixed tree and the last block to arrive
-// sums the block partials in a fixed order, so results are deterministic.
+// flag between batches.  Vectors are T = double or float; scalars and dot
+// products are always accumulated in double.  Reductions are two-level with a
+// fixed grid (elx_reduce.cuh), so results are deterministic.
+//
+// Mixed precision (refinement kernels below): with x = 0 and r = b in FP64,
+// repeat { r32 = r; solve K32 d = r32 by FP32 PCG to a loose tolerance;
+// x += d in FP64; r = b - K x with the FP64 SpMV } until the reference's
+// test ||r||_M < tol ||b||_M holds in FP64.
 #include "elx_krylov.h"
 #include "elx_reduce.cuh"
 
@@ -24,27 +29,30 @@ namespace {
 // ------------------------------------------------------------ kernels
 __global__ void __launch_bounds__(kThreads)
 diag_inverse_kernel(int n, const double *__restrict__ ad, double *__restrict__ m,
-                    int32_t *zero_row) {
+                    float *__restrict__ m32, int32_t *zero_row) {
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const double a = ad[i];
     if (a == 0.0) atomicMin(zero_row, i + 1);
-    m[i] = 1.0 / a;
+    const double mi = 1.0 / a;
+    m[i] = mi;
+    if (m32) m32[i] = (float)mi;
   }
 }
 
 // x = 0, r = b, p = M b and d = (b, M b); conv = tol * sqrt|d| (Iters.f:343-360
 // with x0 = 0, for which K x0 = 0 and r0 = b exactly).
+template <class T>
 __global__ void __launch_bounds__(kThreads)
-pcg_start_kernel(int n, const double *__restrict__ b, const double *__restrict__ m,
-                 double *__restrict__ x, double *__restrict__ r, double *__restrict__ p,
-                 PcgScalars *sc, double *partials, unsigned int *counter) {
+pcg_start_kernel(int n, const T *__restrict__ b, const T *__restrict__ m, T *__restrict__ x,
+                 T *__restrict__ r, T *__restrict__ p, PcgScalars *sc, double *partials,
+                 unsigned int *counter) {
   double v[1] = {0.0};
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    const double bi = b[i], zi = bi * m[i];
-    x[i] = 0.0;
+    const T bi = b[i], zi = bi * m[i];
+    x[i] = T(0);
     r[i] = bi;
     p[i] = zi;
-    v[0] += bi * zi;
+    v[0] += (double)bi * (double)zi;
   }
   block_sum<1>(v);
   if (!publish_partials<1>(v, partials, counter)) return;
@@ -62,8 +70,8 @@ pcg_start_kernel(int n, const double *__restrict__ b, const double *__restrict__
   }
 }
 
-// Second launch of the SpMV (spmv.cu): y(i) = ytile(i) + its halo slots in
-// tile order, in place.  With sc != nullptr it also forms (p, y) and
+// Second launch of the tiled SpMV (spmv.cu): y(i) = ytile(i) + its halo slots
+// in tile order, in place.  With sc != nullptr it also forms (p, y) and
 // alpha = d / (p, y) for the PCG (Iters.f:366-372).
 __global__ void __launch_bounds__(kThreads)
 halo_dot_kernel(int neq, const int32_t *__restrict__ halo_ptr,
@@ -90,19 +98,19 @@ halo_dot_kernel(int neq, const int32_t *__restrict__ halo_ptr,
 }
 
 // x += alpha p; r -= alpha q; (r, M r); beta, d, stopping test.
+template <class T>
 __global__ void __launch_bounds__(kThreads)
-pcg_update_kernel(int n, const double *__restrict__ p, const double *__restrict__ q,
-                  const double *__restrict__ m, double *__restrict__ x,
-                  double *__restrict__ r, PcgScalars *sc, double *partials,
-                  unsigned int *counter) {
+pcg_update_kernel(int n, const T *__restrict__ p, const T *__restrict__ q,
+                  const T *__restrict__ m, T *__restrict__ x, T *__restrict__ r,
+                  PcgScalars *sc, double *partials, unsigned int *counter) {
   if (sc->done) return;
-  const double alpha = sc->alpha;
+  const T alpha = (T)sc->alpha;
   double v[1] = {0.0};
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     x[i] += alpha * p[i];
-    const double ri = r[i] - alpha * q[i];
+    const T ri = r[i] - alpha * q[i];
     r[i] = ri;
-    v[0] += ri * (ri * m[i]);
+    v[0] += (double)ri * (double)(ri * m[i]);
   }
   block_sum<1>(v);
   if (!publish_partials<1>(v, partials, counter)) return;
@@ -124,11 +132,12 @@ pcg_update_kernel(int n, const double *__restrict__ p, const double *__restrict_
 }
 
 // p = M r + beta p.
+template <class T>
 __global__ void __launch_bounds__(kThreads)
-pcg_direction_kernel(int n, const double *__restrict__ r, const double *__restrict__ m,
-                     double *__restrict__ p, const PcgScalars *sc) {
+pcg_direction_kernel(int n, const T *__restrict__ r, const T *__restrict__ m, T *__restrict__ p,
+                     const PcgScalars *sc) {
   if (sc->done) return;
-  const double beta = sc->beta;
+  const T beta = (T)sc->beta;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
     p[i] = r[i] * m[i] + beta * p[i];
 }
@@ -155,7 +164,192 @@ diagnostics_kernel(int n, const double *__restrict__ x, const double *__restrict
     for (int i = 0; i < 4; i++) out[i] = tot[i];
 }
 
+// Refinement residual: r = b - z (z = K x in FP64), r32 = (float) r, and
+// (r, M r) into out[0].  With z == nullptr (x = 0) r = b.
+__global__ void __launch_bounds__(kThreads)
+refine_residual_kernel(int n, const double *__restrict__ b, const double *__restrict__ z,
+                       const double *__restrict__ m, double *__restrict__ r,
+                       float *__restrict__ r32, double *out, double *partials,
+                       unsigned int *counter) {
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double ri = z ? b[i] - z[i] : b[i];
+    r[i] = ri;
+    r32[i] = (float)ri;
+    v[0] += ri * (ri * m[i]);
+  }
+  block_sum<1>(v);
+  if (!publish_partials<1>(v, partials, counter)) return;
+  double tot[1];
+  gather_partials<1>(tot, partials, counter);
+  if (threadIdx.x == 0) out[0] = tot[0];
+}
+
+__global__ void __launch_bounds__(kThreads)
+convert_kernel(int n, const double *__restrict__ src, float *__restrict__ dst) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+    dst[i] = (float)src[i];
+}
+
+__global__ void __launch_bounds__(kThreads)
+widen_kernel(int n, const float *__restrict__ src, double *__restrict__ dst) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+    dst[i] = (double)src[i];
+}
+
+// x += d (the FP32 correction), in FP64.
+__global__ void __launch_bounds__(kThreads)
+refine_accumulate_kernel(int n, double *__restrict__ x, const float *__restrict__ d, int first) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+    x[i] = first ? (double)d[i] : x[i] + (double)d[i];
+}
+
+// ---------------------------------------------------- reliable updates
+// Mixed-precision CG with reliable updates (residual replacement): one FP32
+// CG whose search direction is never restarted; the FP32 solution piece xlo
+// is folded into the FP64 solution and the FP32 residual replaced by the
+// true FP64 residual b - K xhi whenever ||r||_M has dropped by delta since
+// the last replacement, or looks converged.  The stopping test is the
+// reference's, on the FP64 residual.
+
+// x_lo = 0, p = M r, rho = (r, M r), rmax = sqrt(rho).  conv is set by the host
+// from the FP64 (b, M b).
+__global__ void __launch_bounds__(kThreads)
+rel_start_kernel(int n, const float *__restrict__ r, const float *__restrict__ m,
+                 float *__restrict__ xlo, float *__restrict__ p, PcgScalars *sc,
+                 double *partials, unsigned int *counter) {
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const float ri = r[i], zi = ri * m[i];
+    xlo[i] = 0.0f;
+    p[i] = zi;
+    v[0] += (double)ri * (double)zi;
+  }
+  block_sum<1>(v);
+  if (!publish_partials<1>(v, partials, counter)) return;
+  double tot[1];
+  gather_partials<1>(tot, partials, counter);
+  if (threadIdx.x == 0) {
+    sc->d = tot[0];
+    sc->rmax = sqrt(fabs(tot[0]));
+    sc->iters = 0;
+    sc->status = 0;
+    sc->update = 0;
+    sc->nupdates = 0;
+    sc->done = (sc->bmb == 0.0 || sc->maxit <= 0) ? 1 : 0;
+    if (sc->maxit <= 0 && sc->bmb != 0.0) sc->status = ELX_ERR_NO_CONVERGENCE;
+  }
+}
+
+// x_lo += alpha p; r -= alpha q; rho = (r, M r); then either the usual beta,
+// or a replacement is flagged (beta comes from the replaced residual).
+__global__ void __launch_bounds__(kThreads)
+rel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__ q,
+                  const float *__restrict__ m, float *__restrict__ xlo, float *__restrict__ r,
+                  PcgScalars *sc, double *partials, unsigned int *counter) {
+  if (sc->done) return;
+  const float alpha = (float)sc->alpha;
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    xlo[i] += alpha * p[i];
+    const float ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    v[0] += (double)ri * (double)(ri * m[i]);
+  }
+  block_sum<1>(v);
+  if (!publish_partials<1>(v, partials, counter)) return;
+  double tot[1];
+  gather_partials<1>(tot, partials, counter);
+  if (threadIdx.x == 0) {
+    const double di = tot[0];
+    const int it = sc->iters + 1;
+    sc->iters = it;
+    const double rn = sqrt(fabs(di));
+    if (!(di == di)) {
+      sc->done = 1;
+      sc->status = ELX_ERR_NO_CONVERGENCE;
+    } else if (rn < sc->delta * sc->rmax || rn < sc->conv || it >= sc->maxit) {
+      sc->update = 1;  // rel_residual_kernel decides, from the FP64 residual
+    } else {
+      sc->beta = di / sc->d;
+      sc->d = di;
+    }
+  }
+}
+
+// When a replacement is due: x_hi += x_lo, x_lo = 0.
+__global__ void __launch_bounds__(kThreads)
+rel_accumulate_kernel(int n, double *__restrict__ xhi, float *__restrict__ xlo,
+                      const PcgScalars *sc) {
+  if (sc->done || !sc->update) return;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    xhi[i] += (double)xlo[i];
+    xlo[i] = 0.0f;
+  }
+}
+
+// When a replacement is due (z = K x_hi in FP64): r_hi = b - z, r = (float)
+// r_hi, rho = (r_hi, M r_hi); stop on the reference's test, else continue
+// with beta from the replaced residual.
+__global__ void __launch_bounds__(kThreads)
+rel_residual_kernel(int n, const double *__restrict__ b, const double *__restrict__ z,
+                    const double *__restrict__ m, double *__restrict__ rhi,
+                    float *__restrict__ r, PcgScalars *sc, double *partials,
+                    unsigned int *counter) {
+  if (sc->done || !sc->update) return;
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const double ri = b[i] - z[i];
+    rhi[i] = ri;
+    r[i] = (float)ri;
+    v[0] += ri * (ri * m[i]);
+  }
+  block_sum<1>(v);
+  if (!publish_partials<1>(v, partials, counter)) return;
+  double tot[1];
+  gather_partials<1>(tot, partials, counter);
+  if (threadIdx.x == 0) {
+    const double di = tot[0];
+    sc->update = 0;
+    sc->nupdates += 1;
+    if (sqrt(fabs(di)) < sc->conv) {
+      sc->done = 1;
+    } else if (sc->iters >= sc->maxit || !(di == di)) {
+      sc->done = 1;
+      sc->status = ELX_ERR_NO_CONVERGENCE;
+    } else {
+      sc->beta = di / sc->d;
+      sc->d = di;
+      sc->rmax = sqrt(fabs(di));
+    }
+  }
+}
+
 }  // namespace
+
+void launch_rel_start(int n, const float *r, const float *m, float *xlo, float *p,
+                      PcgScalars *sc, double *partials, unsigned int *counter, cudaStream_t st) {
+  rel_start_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, r, m, xlo, p, sc, partials, counter);
+  ELX_CUDA(cudaGetLastError());
+}
+
+// One reliable-update iteration: 6 kernels, the middle three gated on the
+// replacement flag.
+void launch_rel_iteration(const CsrcDev &k, const double *b, const double *m, double *xhi,
+                          double *rhi, double *z, float *xlo, float *r, float *p, float *q,
+                          const float *m32, PcgScalars *sc, double *partials,
+                          unsigned int *counters, cudaStream_t st) {
+  const int n = k.neq;
+  launch_gather_spmv32(k, p, q, sc, partials, counters + 0, st);
+  rel_update_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, p, q, m32, xlo, r, sc, partials,
+                                                         counters + 1);
+  rel_accumulate_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, xhi, xlo, sc);
+  launch_gather_spmv64(k, xhi, z, nullptr, nullptr, nullptr, st, &sc->update);
+  rel_residual_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, b, z, m, rhi, r, sc, partials,
+                                                           counters + 5);
+  pcg_direction_kernel<float><<<vector_grid(n), kThreads, 0, st>>>(n, r, m32, p, sc);
+  ELX_CUDA(cudaGetLastError());
+}
 
 int vector_grid(int n) {
   // a fixed multiple of the SM count keeps the partial count small and fixed
@@ -163,16 +357,25 @@ int vector_grid(int n) {
   return g < 1216 ? (g < 1 ? 1 : g) : 1216;
 }
 
-void launch_diag_inverse(int n, const double *ad, double *m, int32_t *zero_row, cudaStream_t st) {
-  diag_inverse_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, ad, m, zero_row);
+void launch_diag_inverse(int n, const double *ad, double *m, float *m32, int32_t *zero_row,
+                         cudaStream_t st) {
+  diag_inverse_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, ad, m, m32, zero_row);
   ELX_CUDA(cudaGetLastError());
 }
 
-void launch_pcg_start(int n, const double *b, const double *m, double *x, double *r, double *p,
-                      PcgScalars *sc, double *partials, unsigned int *counter, cudaStream_t st) {
-  pcg_start_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, b, m, x, r, p, sc, partials, counter);
+template <class T>
+void launch_pcg_start(int n, const T *b, const T *m, T *x, T *r, T *p, PcgScalars *sc,
+                      double *partials, unsigned int *counter, cudaStream_t st) {
+  pcg_start_kernel<T><<<vector_grid(n), kThreads, 0, st>>>(n, b, m, x, r, p, sc, partials,
+                                                           counter);
   ELX_CUDA(cudaGetLastError());
 }
+template void launch_pcg_start<double>(int, const double *, const double *, double *, double *,
+                                       double *, PcgScalars *, double *, unsigned int *,
+                                       cudaStream_t);
+template void launch_pcg_start<float>(int, const float *, const float *, float *, float *,
+                                      float *, PcgScalars *, double *, unsigned int *,
+                                      cudaStream_t);
 
 void launch_pcg_iteration(const CsrcDev &k, const TileDev &td, int spmv_kind, double *x,
                           double *r, double *p, double *q, double *part, const double *m,
@@ -186,13 +389,24 @@ void launch_pcg_iteration(const CsrcDev &k, const TileDev &td, int spmv_kind, do
   } else {
     launch_gather_spmv64(k, p, q, sc, partials, counters + 0, st);
   }
-  pcg_update_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, p, q, m, x, r, sc, partials,
-                                                         counters + 1);
-  pcg_direction_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, r, m, p, sc);
+  pcg_update_kernel<double><<<vector_grid(n), kThreads, 0, st>>>(n, p, q, m, x, r, sc, partials,
+                                                                 counters + 1);
+  pcg_direction_kernel<double><<<vector_grid(n), kThreads, 0, st>>>(n, r, m, p, sc);
   ELX_CUDA(cudaGetLastError());
 }
 
-// y = K x with the PCG's own two SpMV launches (no dot).
+void launch_pcg_iteration32(const CsrcDev &k, float *x, float *r, float *p, float *q,
+                            const float *m, PcgScalars *sc, double *partials,
+                            unsigned int *counters, cudaStream_t st) {
+  const int n = k.neq;
+  launch_gather_spmv32(k, p, q, sc, partials, counters + 0, st);
+  pcg_update_kernel<float><<<vector_grid(n), kThreads, 0, st>>>(n, p, q, m, x, r, sc, partials,
+                                                                counters + 1);
+  pcg_direction_kernel<float><<<vector_grid(n), kThreads, 0, st>>>(n, r, m, p, sc);
+  ELX_CUDA(cudaGetLastError());
+}
+
+// y = K x with the PCG's own SpMV launches (no dot).
 void launch_spmv64(const CsrcDev &k, const TileDev &td, int spmv_kind, const double *x, double *y,
                    double *part, int32_t *err, cudaStream_t st) {
   if (spmv_kind == kSpmvTiled) {
@@ -210,6 +424,29 @@ void launch_diagnostics(int n, const double *x, const double *z, const double *b
                         const double *m, double *out, double *partials, unsigned int *counter,
                         cudaStream_t st) {
   diagnostics_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, x, z, b, m, out, partials, counter);
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_refine_residual(int n, const double *b, const double *z, const double *m, double *r,
+                            float *r32, double *out, double *partials, unsigned int *counter,
+                            cudaStream_t st) {
+  refine_residual_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, b, z, m, r, r32, out, partials,
+                                                              counter);
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_convert(int n, const double *src, float *dst, cudaStream_t st) {
+  convert_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, src, dst);
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_widen(int n, const float *src, double *dst, cudaStream_t st) {
+  widen_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, src, dst);
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_refine_accumulate(int n, double *x, const float *d, bool first, cudaStream_t st) {
+  refine_accumulate_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, x, d, first ? 1 : 0);
   ELX_CUDA(cudaGetLastError());
 }
 

@@ -259,8 +259,10 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
                    const T *__restrict__ al, const int32_t *__restrict__ iat,
                    const int32_t *__restrict__ jat, const T *__restrict__ alt,
                    const T *__restrict__ ad, const T *__restrict__ x, T *__restrict__ y,
-                   PcgScalars *sc, double *partials, unsigned int *counter) {
+                   PcgScalars *sc, double *partials, unsigned int *counter,
+                   const int32_t *gate) {
   if (DOT && sc->done) return;
+  if (gate && *gate == 0) return;  // conditional product (mixed-precision replacement)
   constexpr int RPB = 256 / LANES;  // rows per block pass
   const int lane = threadIdx.x % LANES, sub = threadIdx.x / LANES;
   double v[1] = {0.0};
@@ -330,12 +332,14 @@ int gather_grid(int neq, int lanes) {
 
 template <class T, bool DOT>
 void launch_gather(const CsrcDev &k, const T *al, const T *alt, const T *ad, const T *x, T *y,
-                   PcgScalars *sc, double *partials, unsigned int *counter, cudaStream_t st) {
+                   PcgScalars *sc, double *partials, unsigned int *counter, cudaStream_t st,
+                   const int32_t *gate = nullptr) {
   // 4 threads per row and 4 entries in flight per thread measured fastest on
   // the 64^3 HEXA8 cube (lanes 2/4/8 x unroll 2/4 swept: 166.8 us vs >= 174 us)
   const int grid = gather_grid(k.neq, 4);
   gather_spmv_kernel<T, 4, 4, DOT><<<grid, 256, 0, st>>>(k.neq, k.ia, k.ja, al, k.iat, k.jat,
-                                                         alt, ad, x, y, sc, partials, counter);
+                                                         alt, ad, x, y, sc, partials, counter,
+                                                         gate);
   ELX_CUDA(cudaGetLastError());
 }
 
@@ -413,15 +417,21 @@ void launch_transpose_values(const CsrcDev &k, cudaStream_t st) {
 }
 
 void launch_gather_spmv64(const CsrcDev &k, const double *x, double *y, PcgScalars *sc,
-                          double *partials, unsigned int *counter, cudaStream_t st) {
+                          double *partials, unsigned int *counter, cudaStream_t st,
+                          const int32_t *gate) {
   if (sc)
-    launch_gather<double, true>(k, k.al, k.alt, k.ad, x, y, sc, partials, counter, st);
+    launch_gather<double, true>(k, k.al, k.alt, k.ad, x, y, sc, partials, counter, st, gate);
   else
-    launch_gather<double, false>(k, k.al, k.alt, k.ad, x, y, nullptr, nullptr, nullptr, st);
+    launch_gather<double, false>(k, k.al, k.alt, k.ad, x, y, nullptr, nullptr, nullptr, st,
+                                 gate);
 }
 
-void launch_gather_spmv32(const CsrcDev &k, const float *x, float *y, cudaStream_t st) {
-  launch_gather<float, false>(k, k.al32, k.alt32, k.ad32, x, y, nullptr, nullptr, nullptr, st);
+void launch_gather_spmv32(const CsrcDev &k, const float *x, float *y, PcgScalars *sc,
+                          double *partials, unsigned int *counter, cudaStream_t st) {
+  if (sc)
+    launch_gather<float, true>(k, k.al32, k.alt32, k.ad32, x, y, sc, partials, counter, st);
+  else
+    launch_gather<float, false>(k, k.al32, k.alt32, k.ad32, x, y, nullptr, nullptr, nullptr, st);
 }
 
 }  // namespace elx
@@ -483,7 +493,8 @@ extern "C" int elx_spmv_dot_noalloc(int32_t neq, const int32_t *ia, const int32_
     return ELX_ERR_CUDA;
   const int grid = (neq + kNoAllocRowsPerBlock - 1) / kNoAllocRowsPerBlock;
   gather_spmv_kernel<double, 4, 4, true, 1><<<grid, 256, 0, st>>>(
-      neq, ia, ja, al, iat, jat, alt, ad, x, y, &sc->scalars, sc->partials, &sc->counter);
+      neq, ia, ja, al, iat, jat, alt, ad, x, y, &sc->scalars, sc->partials, &sc->counter,
+      nullptr);
   if (cudaGetLastError() != cudaSuccess) return ELX_ERR_CUDA;
   if (cudaMemcpyAsync(xy, &sc->scalars.pq, sizeof(double), cudaMemcpyDeviceToDevice, st) !=
       cudaSuccess)

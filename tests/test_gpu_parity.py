@@ -206,3 +206,38 @@ def test_full_size_cube_solve_properties(gpu_ctx):
     np.testing.assert_allclose(info["xkx"], b @ x, rtol=1e-6)
     x2, info2 = gpu_ctx.solve(b, tol=1e-8, maxit=20000)
     assert np.array_equal(x, x2)
+
+
+# ------------------------------------------------------------ mixed precision
+FP32_SPMV_TOL = 1e-6
+
+
+@pytest.mark.parametrize("name", ["quad4_stress", "tetra4", "hexa8"])
+def test_fp32_spmv_parity(gpu_ctx, name):
+    """The FP32 product of the mixed-precision inner iteration, against the
+    FP64 oracle (FP32 values and vectors: relative error near 1e-7)."""
+    m = MESHES[name]()
+    s = _setup(gpu_ctx, m)
+    _, ad, al = gpu_ctx.assemble(None, None, want_matrix=True)
+    x = np.random.default_rng(3).standard_normal(s.neq)
+    y_o = O.matvec(s, ad, al, x)
+    y_g = gpu_ctx.spmv(x, precision=E.PREC_MIXED)
+    assert rel_inf(y_o, y_g) <= FP32_SPMV_TOL
+
+
+@pytest.mark.parametrize("name", ["quad4_stress", "tetra4", "hexa8"])
+def test_mixed_precision_refinement_matches_fp64(gpu_ctx, name):
+    """FP32 inner PCG + FP64 refinement meets the reference's FP64 stopping
+    test, and its solution agrees with the FP64 oracle's PCG solution to the
+    accuracy both solves carry (tolerance 1e-10)."""
+    m = MESHES[name]()
+    m.f = np.random.default_rng(7).standard_normal(m.f.shape) * (m.id == 0)
+    s = _setup(gpu_ctx, m)
+    b0, u0 = O.loads(m, s)
+    ad, al, b = O.assemble(m, s, u0, b0)
+    x_o, i_o = O.pcg(s, ad, al, b, tol=1e-10, maxit=20000)
+    gpu_ctx.assemble(u0, b0)
+    x_g, i_g = gpu_ctx.solve(b, tol=1e-10, maxit=20000, precision=E.PREC_MIXED)
+    assert i_g["status"] == 0 and i_g["refinements"] >= 1
+    assert i_g["norm_m_r"] <= i_g["conv"] * (1 + 1e-6)
+    assert rel_inf(x_o, x_g) <= 1e-7
