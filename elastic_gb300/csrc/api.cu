@@ -26,12 +26,13 @@ struct elx_ctx {
 
   // mesh (colour order) and structure
   DBuf conn, mat, elnum, slot, x, eq, e;
-  DBuf ia, ja, iat, jat, pt;
+  DBuf ia, ja, iat, jat, pt, ja16, jat16;
   // tiled transposed index of the SpMV and its halo slots
   DBuf tile_tgt, tile_out, tgt_col, tgt_start, tpos, halo_ptr, halo_slot, tile_desc, part;
   // matrix
   DBuf ad, al, alt, ad32, al32, alt32;
   int spmv_kind = elx::kSpmvGather;  // FP64 SpMV kernel family
+  bool use_delta = true;             // 16-bit column deltas when the bandwidth fits
   // state and solver vectors
   DBuf u, b0, b, xs, r, p, q, m, z;
   // mixed precision: FP32 inner PCG vectors and preconditioner
@@ -101,6 +102,8 @@ struct elx_ctx {
     k.neq = s.neq; k.nad = s.nad;
     k.ia = ia.as<int32_t>(); k.ja = ja.as<int32_t>();
     k.iat = iat.as<int32_t>(); k.jat = jat.as<int32_t>(); k.pt = pt.as<int32_t>();
+    k.ja16 = s.bw16 && use_delta ? ja16.as<uint16_t>() : nullptr;
+    k.jat16 = s.bw16 && use_delta ? jat16.as<uint16_t>() : nullptr;
     k.ad = ad.as<double>(); k.al = al.as<double>(); k.alt = alt.as<double>();
     k.ad32 = ad32.as<float>(); k.al32 = al32.as<float>(); k.alt32 = alt32.as<float>();
     return k;
@@ -201,6 +204,14 @@ void upload_structure(elx_ctx *c) {
   c->upload(c->iat, s.iat.data(), s.iat.size());
   c->upload(c->jat, s.jat.data(), s.jat.size());
   c->upload(c->pt, s.pt.data(), s.pt.size());
+  if (s.bw16) {
+    c->upload(c->ja16, s.ja16.data(), s.ja16.size());
+    c->upload(c->jat16, s.jat16.data(), s.jat16.size());
+  } else {
+    c->release(c->ja16);
+    c->release(c->jat16);
+  }
+  if (const char *env = getenv("ELX_DELTA16")) c->use_delta = atoi(env) != 0;
   if (const char *env = getenv("ELX_SPMV"))
     c->spmv_kind = std::string(env) == "tile" ? elx::kSpmvTiled : elx::kSpmvGather;
   c->upload(c->tile_tgt, s.tile_tgt.data(), s.tile_tgt.size());
@@ -300,7 +311,8 @@ void build_preconditioner(elx_ctx *c) {
                                        std::to_string(c->h_flags[1])};
 }
 
-constexpr int kBatch = 16;  // PCG iterations per captured graph launch
+constexpr int kBatch = 16;        // PCG iterations per captured graph launch
+constexpr int kReplaceEvery = 4;  // mixed precision: replacement check interval
 
 // Captures kBatch iterations (FP64 or the FP32 inner iteration) as a graph.
 cudaGraphExec_t capture_batch(elx_ctx *c, bool fp32) {
@@ -316,7 +328,7 @@ cudaGraphExec_t capture_batch(elx_ctx *c, bool fp32) {
                                   c->r32.as<float>(), c->p32.as<float>(), c->q32.as<float>(),
                                   c->m32.as<float>(), c->scal.as<elx::PcgScalars>(),
                                   c->partials.as<double>(), c->counters.as<unsigned int>(),
-                                  c->stream);
+                                  i % kReplaceEvery == kReplaceEvery - 1, c->stream);
       else
         elx::launch_pcg_iteration(k, td, c->spmv_kind, c->xs.as<double>(), c->r.as<double>(),
                                   c->p.as<double>(), c->q.as<double>(), c->part.as<double>(),
@@ -343,13 +355,13 @@ void capture_pcg_graph(elx_ctx *c) {
 
 // Launches batches of `graph` until the scalars' stopping flag is set (two
 // batches in flight; the host reads the flag of the older one).
-elx::PcgScalars run_batches(elx_ctx *c, cudaGraphExec_t graph, int kernels_per_iter,
+elx::PcgScalars run_batches(elx_ctx *c, cudaGraphExec_t graph, double kernels_per_iter,
                             int maxit) {
   elx::PcgScalars *d_sc = c->scal.as<elx::PcgScalars>();
   int launched = 0, checked = 0;
   auto launch_batch = [&](int slot) {
     ELX_CUDA(cudaGraphLaunch(graph, c->stream));
-    c->launches += (int64_t)kernels_per_iter * kBatch;
+    c->launches += (int64_t)(kernels_per_iter * kBatch + 0.5);
     ELX_CUDA(cudaMemcpyAsync(&c->h_scal[slot], d_sc, sizeof(elx::PcgScalars),
                              cudaMemcpyDeviceToHost, c->stream));
     ELX_CUDA(cudaEventRecord(c->ev[slot], c->stream));
@@ -480,7 +492,7 @@ void pcg_mixed(elx_ctx *c, double tol, int maxit, elx_info *info) {
                         c->p32.as<float>(), c->scal.as<elx::PcgScalars>(),
                         c->partials.as<double>(), c->counters.as<unsigned int>() + 2, c->stream);
   c->launches += 2;
-  elx::PcgScalars last = run_batches(c, c->pcg32_graph, 6, maxit);
+  elx::PcgScalars last = run_batches(c, c->pcg32_graph, 3 + 3.0 / kReplaceEvery, maxit);
   // fold the last FP32 piece (zero unless maxit stopped the iteration)
   elx::launch_refine_accumulate(n, c->xs.as<double>(), c->x32.as<float>(), false, c->stream);
   c->launches += 1;
@@ -612,7 +624,8 @@ void elx_destroy(elx_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->drop_graphs();
   for (DBuf *d : {&c->conn, &c->mat, &c->elnum, &c->slot, &c->x, &c->eq, &c->e, &c->ia, &c->ja,
-                  &c->iat, &c->jat, &c->pt, &c->alt, &c->alt32, &c->tile_tgt, &c->tile_out, &c->tgt_col, &c->tgt_start, &c->tpos,
+                  &c->iat, &c->jat, &c->pt, &c->ja16, &c->jat16, &c->alt, &c->alt32,
+                  &c->tile_tgt, &c->tile_out, &c->tgt_col, &c->tgt_start, &c->tpos,
                   &c->halo_ptr, &c->halo_slot, &c->tile_desc, &c->part, &c->ad, &c->al,
                   &c->ad32, &c->al32,
                   &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,

@@ -99,6 +99,10 @@ struct Structure {
   // part): for each row c the entries of column c of L, by ascending row:
   // their rows jat and their positions pt in al.
   std::vector<int32_t> iat, jat, pt;
+  // 16-bit column deltas of both parts (row - col below, col - row above),
+  // used when the matrix bandwidth fits (bw16 = true)
+  bool bw16 = false;
+  std::vector<uint16_t> ja16, jat16;
 };
 
 // host structure routines (structure.cpp)
@@ -135,6 +139,7 @@ struct CsrcDev {
   const int32_t *iat;  // (neq+1) upper part (transposed index) row pointers
   const int32_t *jat;  // (nad)   upper part columns
   const int32_t *pt;   // (nad)   position in al of each upper entry
+  const uint16_t *ja16, *jat16;  // 16-bit column deltas (null: use ja/jat)
   double *ad, *al, *alt;
   float *ad32, *al32, *alt32;
 };

@@ -54,7 +54,7 @@ void launch_rel_start(int n, const float *r, const float *m, float *xlo, float *
 void launch_rel_iteration(const CsrcDev &k, const double *b, const double *m, double *xhi,
                           double *rhi, double *z, float *xlo, float *r, float *p, float *q,
                           const float *m32, PcgScalars *sc, double *partials,
-                          unsigned int *counters, cudaStream_t st);
+                          unsigned int *counters, bool replacement_point, cudaStream_t st);
 void launch_convert(int n, const double *src, float *dst, cudaStream_t st);
 void launch_widen(int n, const float *src, double *dst, cudaStream_t st);
 

@@ -241,8 +241,10 @@ rel_start_kernel(int n, const float *__restrict__ r, const float *__restrict__ m
   }
 }
 
-// x_lo += alpha p; r -= alpha q; rho = (r, M r); then either the usual beta,
-// or a replacement is flagged (beta comes from the replaced residual).
+// x_lo += alpha p; r -= alpha q; rho = (r, M r); beta; and the replacement
+// flag when ||r||_M has dropped by delta since the last replacement, looks
+// converged, or maxit is reached (rel_residual_kernel then decides, from the
+// FP64 residual, at the next replacement point).
 __global__ void __launch_bounds__(kThreads)
 rel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__ q,
                   const float *__restrict__ m, float *__restrict__ xlo, float *__restrict__ r,
@@ -268,12 +270,11 @@ rel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__ 
     if (!(di == di)) {
       sc->done = 1;
       sc->status = ELX_ERR_NO_CONVERGENCE;
-    } else if (rn < sc->delta * sc->rmax || rn < sc->conv || it >= sc->maxit) {
-      sc->update = 1;  // rel_residual_kernel decides, from the FP64 residual
-    } else {
-      sc->beta = di / sc->d;
-      sc->d = di;
+      return;
     }
+    sc->beta = di / sc->d;
+    sc->d = di;
+    if (rn < sc->delta * sc->rmax || rn < sc->conv || it >= sc->maxit) sc->update = 1;
   }
 }
 
@@ -290,7 +291,7 @@ rel_accumulate_kernel(int n, double *__restrict__ xhi, float *__restrict__ xlo,
 
 // When a replacement is due (z = K x_hi in FP64): r_hi = b - z, r = (float)
 // r_hi, rho = (r_hi, M r_hi); stop on the reference's test, else continue
-// with beta from the replaced residual.
+// (the search direction is kept; the next alpha uses the replaced rho).
 __global__ void __launch_bounds__(kThreads)
 rel_residual_kernel(int n, const double *__restrict__ b, const double *__restrict__ z,
                     const double *__restrict__ m, double *__restrict__ rhi,
@@ -318,7 +319,6 @@ rel_residual_kernel(int n, const double *__restrict__ b, const double *__restric
       sc->done = 1;
       sc->status = ELX_ERR_NO_CONVERGENCE;
     } else {
-      sc->beta = di / sc->d;
       sc->d = di;
       sc->rmax = sqrt(fabs(di));
     }
@@ -333,21 +333,24 @@ void launch_rel_start(int n, const float *r, const float *m, float *xlo, float *
   ELX_CUDA(cudaGetLastError());
 }
 
-// One reliable-update iteration: 6 kernels, the middle three gated on the
-// replacement flag.
+// One reliable-update iteration: the FP32 CG step (3 kernels), and at
+// replacement points (every few iterations) three more kernels that run only
+// when the replacement flag is set.
 void launch_rel_iteration(const CsrcDev &k, const double *b, const double *m, double *xhi,
                           double *rhi, double *z, float *xlo, float *r, float *p, float *q,
                           const float *m32, PcgScalars *sc, double *partials,
-                          unsigned int *counters, cudaStream_t st) {
+                          unsigned int *counters, bool replacement_point, cudaStream_t st) {
   const int n = k.neq;
   launch_gather_spmv32(k, p, q, sc, partials, counters + 0, st);
   rel_update_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, p, q, m32, xlo, r, sc, partials,
                                                          counters + 1);
-  rel_accumulate_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, xhi, xlo, sc);
-  launch_gather_spmv64(k, xhi, z, nullptr, nullptr, nullptr, st, &sc->update);
-  rel_residual_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, b, z, m, rhi, r, sc, partials,
-                                                           counters + 5);
   pcg_direction_kernel<float><<<vector_grid(n), kThreads, 0, st>>>(n, r, m32, p, sc);
+  if (replacement_point) {
+    rel_accumulate_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, xhi, xlo, sc);
+    launch_gather_spmv64(k, xhi, z, nullptr, nullptr, nullptr, st, &sc->update);
+    rel_residual_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, b, z, m, rhi, r, sc, partials,
+                                                             counters + 5);
+  }
   ELX_CUDA(cudaGetLastError());
 }
 

@@ -252,15 +252,18 @@ spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32
 // Rows are walked with a fixed grid so that the optional dot (x, y) reduces
 // in a fixed order.
 // BASE is the index base of ia/ja/iat/jat contents (0 inside the library,
-// 1 for arrays in the reference's 1-based convention).
-template <class T, int LANES, int U, bool DOT, int BASE = 0>
+// 1 for arrays in the reference's 1-based convention).  With DELTA the
+// columns come as 16-bit distances from the row (ja16: row - col below the
+// diagonal, jat16: col - row above it): 2 bytes per stored entry instead of 4.
+template <class T, int LANES, int U, bool DOT, int BASE = 0, bool DELTA = false>
 __global__ void __launch_bounds__(256)
 gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__restrict__ ja,
                    const T *__restrict__ al, const int32_t *__restrict__ iat,
                    const int32_t *__restrict__ jat, const T *__restrict__ alt,
                    const T *__restrict__ ad, const T *__restrict__ x, T *__restrict__ y,
                    PcgScalars *sc, double *partials, unsigned int *counter,
-                   const int32_t *gate) {
+                   const int32_t *gate, const uint16_t *__restrict__ ja16 = nullptr,
+                   const uint16_t *__restrict__ jat16 = nullptr) {
   if (DOT && sc->done) return;
   if (gate && *gate == 0) return;  // conditional product (mixed-precision replacement)
   constexpr int RPB = 256 / LANES;  // rows per block pass
@@ -273,6 +276,7 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
 #pragma unroll
       for (int part = 0; part < 2; part++) {
         const int32_t *cols = part ? jat : ja;
+        const uint16_t *dels = part ? jat16 : ja16;
         const T *vals = part ? alt : al;
         const int kb = (part ? iat[row] : ia[row]) - BASE;
         const int ke = (part ? iat[row + 1] : ia[row + 1]) - BASE;
@@ -283,7 +287,10 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
           for (int u = 0; u < U; u++) {
             const int k = k0 + u * LANES;
             a[u] = k < ke ? vals[k] : T(0);
-            j[u] = k < ke ? cols[k] - BASE : row;
+            if (DELTA)
+              j[u] = k < ke ? (part ? row + (int)dels[k] : row - (int)dels[k]) : row;
+            else
+              j[u] = k < ke ? cols[k] - BASE : row;
           }
 #pragma unroll
           for (int u = 0; u < U; u++) xv[u] = x[j[u]];
@@ -337,9 +344,14 @@ void launch_gather(const CsrcDev &k, const T *al, const T *alt, const T *ad, con
   // 4 threads per row and 4 entries in flight per thread measured fastest on
   // the 64^3 HEXA8 cube (lanes 2/4/8 x unroll 2/4 swept: 166.8 us vs >= 174 us)
   const int grid = gather_grid(k.neq, 4);
-  gather_spmv_kernel<T, 4, 4, DOT><<<grid, 256, 0, st>>>(k.neq, k.ia, k.ja, al, k.iat, k.jat,
-                                                         alt, ad, x, y, sc, partials, counter,
-                                                         gate);
+  if (k.ja16)
+    gather_spmv_kernel<T, 4, 4, DOT, 0, true><<<grid, 256, 0, st>>>(
+        k.neq, k.ia, k.ja, al, k.iat, k.jat, alt, ad, x, y, sc, partials, counter, gate, k.ja16,
+        k.jat16);
+  else
+    gather_spmv_kernel<T, 4, 4, DOT><<<grid, 256, 0, st>>>(k.neq, k.ia, k.ja, al, k.iat, k.jat,
+                                                           alt, ad, x, y, sc, partials, counter,
+                                                           gate);
   ELX_CUDA(cudaGetLastError());
 }
 

@@ -498,13 +498,28 @@ void build_transpose(Structure &s) {
   s.jat.assign(s.nad, 0);
   s.pt.assign(s.nad, 0);
   std::vector<int32_t> fill(s.iat.begin(), s.iat.end() - 1);
+  int32_t bw = 0;
   for (int r = 0; r < neq; r++)
     for (int32_t k = s.ia[r] - 1; k < s.ia[r + 1] - 1; k++) {
       const int c = s.ja[k] - 1;
       const int32_t q = fill[c]++;
       s.jat[q] = r;
       s.pt[q] = k;
+      bw = std::max(bw, r - c);
     }
+  // 16-bit deltas when every |row - col| fits (typical after RCM)
+  s.bw16 = bw <= 65535;
+  s.ja16.clear();
+  s.jat16.clear();
+  if (s.bw16) {
+    s.ja16.resize(s.nad);
+    s.jat16.resize(s.nad);
+    for (int r = 0; r < neq; r++) {
+      for (int32_t k = s.ia[r] - 1; k < s.ia[r + 1] - 1; k++)
+        s.ja16[k] = (uint16_t)(r - (s.ja[k] - 1));
+      for (int32_t q = s.iat[r]; q < s.iat[r + 1]; q++) s.jat16[q] = (uint16_t)(s.jat[q] - r);
+    }
+  }
 }
 
 }  // namespace elx
