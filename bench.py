@@ -142,12 +142,12 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per SpMV launch from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "spmv_fp64_hexa8_cube64.md")
+def profiled(key, name="gather_spmv_fp64_hexa8_cube64.md"):
+    """A figure (`key: value` line) from a committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
-    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
+    m = re.search(key + r":\s*([0-9.eE+]+)", open(p).read())
     return float(m.group(1)) if m else None
 
 
@@ -204,23 +204,46 @@ def run_ours(args, dist: Dist):
     ms_step = ms_total / args.steps
     iters = infos[-1]["iters"]
 
-    # ---- SpMV (the dominant kernel) timed alone on the same stream
-    reps = 50
-    ctx.spmv_resident(reps=5)
-    torch.cuda.synchronize(dev)
-    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s0.record(ext)
-    ctx.spmv_resident(reps=reps)
-    s1.record(ext)
-    torch.cuda.synchronize(dev)
-    clk = clocks.stop()
-    spmv_ms = s0.elapsed_time(s1) / reps
+    x64 = ctx.solution()
+
+    # ---- the SpMV as the solver launches it (the dominant kernel), timed on
+    # its own stream; the matrix (400 MB FP64, 252 MB FP32 two-sided) is
+    # larger than L2, so every launch streams it from HBM
+    def time_spmv(prec, reps=50):
+        ctx.spmv_resident(precision=prec, reps=5)
+        torch.cuda.synchronize(dev)
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(ext)
+        ctx.spmv_resident(precision=prec, reps=reps)
+        s1.record(ext)
+        torch.cuda.synchronize(dev)
+        return s0.elapsed_time(s1) / reps
+
+    spmv_ms = time_spmv(E.PREC_FP64)
     spmv_bytes = 12 * nad + 28 * neq
     spmv_gbs = spmv_bytes / (spmv_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     iter_bytes = 12 * nad + 116 * neq
     pcg_ms = ms_step - asm_ms
     iter_gbs = iter_bytes * iters / (pcg_ms * 1e-3) / 1e9
+
+    # ---- the same step with the mixed-precision solver (FP32 inner PCG with
+    # FP64 reliable updates, the FP64 stopping test)
+    mixed_ms, minfo = [], None
+    for k in range(args.warmup + args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        ctx.assemble_resident()
+        minfo = ctx.solve_resident(precision=E.PREC_MIXED, tol=TOL, maxit=MAXIT)
+        e1.record(ext)
+        torch.cuda.synchronize(dev)
+        if k >= args.warmup:
+            mixed_ms.append(e0.elapsed_time(e1))
+    xm = ctx.solution()
+    spmv32_ms = time_spmv(E.PREC_MIXED)
+    spmv32_bytes = 8 * nad + 16 * neq
+    clk = clocks.stop()
+    mixed_step = dist.max(statistics.median(mixed_ms))
 
     # ---- end to end through the C ABI with host buffers (pinned)
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
@@ -253,11 +276,21 @@ def run_ours(args, dist: Dist):
             "time_to_tol_ms": ms_step, "pcg_iters": iters, "assembly_ms": asm_ms,
             "pcg_ms": pcg_ms, "pcg_iter_gbs": iter_gbs, "spmv_ms": spmv_ms,
             "spmv_gbs": spmv_gbs, "wall_s": wall,
-            "roofline": {"bound": "hbm", "kernel": "pcg_spmv_dot_kernel (FP64 CSRC SpMV)",
+            "roofline": {"bound": "hbm",
+                         "kernel": "gather_spmv_kernel<double> (FP64 CSRC SpMV + fused (p, Kp))",
                          "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
                          "frac": spmv_gbs / peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": spmv_bytes,
-                         "traffic": profiled_traffic()},
+                         "traffic": profiled("traffic_bytes_per_launch"),
+                         "fp64_pipe_frac_ncu": profiled("fp64_pipe_frac")},
+            "mixed": {"ms_per_step": mixed_step, "solves_per_s": n * 1000.0 / mixed_step,
+                      "speedup_vs_fp64": ms_step / mixed_step,
+                      "pcg_iters": minfo["iters"], "refinements": minfo["refinements"],
+                      "rel_err_vs_fp64": float(np.abs(xm - x64).max() / np.abs(x64).max()),
+                      "norm_m_r": minfo["norm_m_r"], "conv": minfo["conv"],
+                      "spmv32_ms": spmv32_ms,
+                      "spmv32_gbs": spmv32_bytes / (spmv32_ms * 1e-3) / 1e9,
+                      "spmv32_frac": spmv32_bytes / (spmv32_ms * 1e-3) / 1e9 / peak},
             "e2e": {"value": n / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,

@@ -890,14 +890,28 @@ int elx_spmv(elx_ctx *c, int32_t precision, const double *x, double *y) {
 int elx_spmv_resident(elx_ctx *c, int32_t precision, int32_t reps) {
   return guarded(c, [&] {
     require(c->have_matrix, ELX_ERR_STATE, "no matrix");
+    // the product as the solvers launch it: q = K p with the fused (p, q)
+    // (fresh scalars, so that no finished-solve flag skips the work)
+    set_scalars(c, 0.0, 0);
+    auto *sc = c->scal.as<elx::PcgScalars>();
     if (precision == ELX_PREC_FP64) {
-      for (int i = 0; i < reps; i++) spmv64(c, c->p.as<double>(), c->q.as<double>());
+      for (int i = 0; i < reps; i++) {
+        if (c->spmv_kind == elx::kSpmvTiled) {
+          spmv64(c, c->p.as<double>(), c->q.as<double>());
+        } else {
+          elx::launch_gather_spmv64(c->csrc_dev(), c->p.as<double>(), c->q.as<double>(), sc,
+                                    c->partials.as<double>(), c->counters.as<unsigned int>(),
+                                    c->stream);
+          c->launches += 1;
+        }
+      }
     } else if (precision == ELX_PREC_MIXED) {
       ensure_fp32(c);
       elx::launch_convert(c->s.neq, c->p.as<double>(), c->p32.as<float>(), c->stream);
       for (int i = 0; i < reps; i++)
-        elx::launch_gather_spmv32(c->csrc_dev(), c->p32.as<float>(), c->q32.as<float>(),
-                                  nullptr, nullptr, nullptr, c->stream);
+        elx::launch_gather_spmv32(c->csrc_dev(), c->p32.as<float>(), c->q32.as<float>(), sc,
+                                  c->partials.as<double>(), c->counters.as<unsigned int>(),
+                                  c->stream);
       c->launches += 1 + reps;
     } else {
       throw Error{ELX_ERR_ARG, "precision not available"};

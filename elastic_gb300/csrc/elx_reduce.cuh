@@ -37,6 +37,31 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
   }
 }
 
+// Block-wide sum of NV per-thread values of type T (float in the FP32
+// kernels): the warp stage adds in T, the per-warp sums are widened to double
+// and added in a fixed order.  Keeps the FP32 kernels off the (narrow) FP64
+// pipe except for a handful of additions per block.  Result in thread 0.
+template <int NV, class T>
+__device__ __forceinline__ void block_sum_widen(const T (&v)[NV], double (&out)[NV]) {
+  __shared__ double sh[NV][kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    const T s = warp_sum(v[i]);
+    if (lane == 0) sh[i][w] = (double)s;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < NV; i++) out[i] = 0.0;
+  if (w == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+      double t = lane < kThreads / 32 ? sh[i][lane] : 0.0;
+      out[i] = warp_sum(t);
+    }
+  }
+}
+
 // Writes this block's NV partials and returns true in thread 0 of the last
 // block to arrive, after which that thread may read every block's partials.
 template <int NV>

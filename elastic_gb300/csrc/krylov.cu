@@ -26,6 +26,20 @@
 namespace elx {
 namespace {
 
+// 16-byte vector of T: the vector kernels stream 16 bytes per load.
+template <class T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+  static constexpr int W = 4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+  static constexpr int W = 2;
+};
+
 // ------------------------------------------------------------ kernels
 __global__ void __launch_bounds__(kThreads)
 diag_inverse_kernel(int n, const double *__restrict__ ad, double *__restrict__ m,
@@ -98,15 +112,36 @@ halo_dot_kernel(int neq, const int32_t *__restrict__ halo_ptr,
 }
 
 // x += alpha p; r -= alpha q; (r, M r); beta, d, stopping test.
+// 16-byte vector loads; the tail of n % W elements is done element-wise.
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 pcg_update_kernel(int n, const T *__restrict__ p, const T *__restrict__ q,
                   const T *__restrict__ m, T *__restrict__ x, T *__restrict__ r,
                   PcgScalars *sc, double *partials, unsigned int *counter) {
   if (sc->done) return;
+  using VT = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::W;
   const T alpha = (T)sc->alpha;
   double v[1] = {0.0};
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+  const int stride = gridDim.x * kThreads, t0 = blockIdx.x * kThreads + threadIdx.x;
+  const int nv = n / W;
+  for (int iv = t0; iv < nv; iv += stride) {
+    VT pv = reinterpret_cast<const VT *>(p)[iv], qv = reinterpret_cast<const VT *>(q)[iv];
+    VT mv = reinterpret_cast<const VT *>(m)[iv], xv = reinterpret_cast<VT *>(x)[iv];
+    VT rv = reinterpret_cast<VT *>(r)[iv];
+    const T *pe = reinterpret_cast<const T *>(&pv), *qe = reinterpret_cast<const T *>(&qv);
+    const T *me = reinterpret_cast<const T *>(&mv);
+    T *xe = reinterpret_cast<T *>(&xv), *re = reinterpret_cast<T *>(&rv);
+#pragma unroll
+    for (int c = 0; c < W; c++) {
+      xe[c] += alpha * pe[c];
+      re[c] = re[c] - alpha * qe[c];
+      v[0] += (double)re[c] * (double)(re[c] * me[c]);
+    }
+    reinterpret_cast<VT *>(x)[iv] = xv;
+    reinterpret_cast<VT *>(r)[iv] = rv;
+  }
+  for (int i = nv * W + t0; i < n; i += stride) {
     x[i] += alpha * p[i];
     const T ri = r[i] - alpha * q[i];
     r[i] = ri;
@@ -131,15 +166,27 @@ pcg_update_kernel(int n, const T *__restrict__ p, const T *__restrict__ q,
   }
 }
 
-// p = M r + beta p.
+// p = M r + beta p (16-byte vector loads).
 template <class T>
 __global__ void __launch_bounds__(kThreads)
 pcg_direction_kernel(int n, const T *__restrict__ r, const T *__restrict__ m, T *__restrict__ p,
                      const PcgScalars *sc) {
   if (sc->done) return;
+  using VT = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::W;
   const T beta = (T)sc->beta;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
-    p[i] = r[i] * m[i] + beta * p[i];
+  const int stride = gridDim.x * kThreads, t0 = blockIdx.x * kThreads + threadIdx.x;
+  const int nv = n / W;
+  for (int iv = t0; iv < nv; iv += stride) {
+    VT rv = reinterpret_cast<const VT *>(r)[iv], mv = reinterpret_cast<const VT *>(m)[iv];
+    VT pv = reinterpret_cast<VT *>(p)[iv];
+    const T *re = reinterpret_cast<const T *>(&rv), *me = reinterpret_cast<const T *>(&mv);
+    T *pe = reinterpret_cast<T *>(&pv);
+#pragma unroll
+    for (int c = 0; c < W; c++) pe[c] = re[c] * me[c] + beta * pe[c];
+    reinterpret_cast<VT *>(p)[iv] = pv;
+  }
+  for (int i = nv * W + t0; i < n; i += stride) p[i] = r[i] * m[i] + beta * p[i];
 }
 
 // Post-solve diagnostics (Iters.f:433-458): z = K x is given; r = b - z;
@@ -251,15 +298,31 @@ rel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__ 
                   PcgScalars *sc, double *partials, unsigned int *counter) {
   if (sc->done) return;
   const float alpha = (float)sc->alpha;
-  double v[1] = {0.0};
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+  float v[1] = {0.0f};  // widened to double per warp
+  const int stride = gridDim.x * kThreads, t0 = blockIdx.x * kThreads + threadIdx.x;
+  const int nv = n / 4;
+  for (int iv = t0; iv < nv; iv += stride) {
+    const float4 pv = reinterpret_cast<const float4 *>(p)[iv];
+    const float4 qv = reinterpret_cast<const float4 *>(q)[iv];
+    const float4 mv = reinterpret_cast<const float4 *>(m)[iv];
+    float4 xv = reinterpret_cast<float4 *>(xlo)[iv];
+    float4 rv = reinterpret_cast<float4 *>(r)[iv];
+    xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+    rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
+    v[0] += rv.x * (rv.x * mv.x) + rv.y * (rv.y * mv.y) + rv.z * (rv.z * mv.z) +
+            rv.w * (rv.w * mv.w);
+    reinterpret_cast<float4 *>(xlo)[iv] = xv;
+    reinterpret_cast<float4 *>(r)[iv] = rv;
+  }
+  for (int i = nv * 4 + t0; i < n; i += stride) {
     xlo[i] += alpha * p[i];
     const float ri = r[i] - alpha * q[i];
     r[i] = ri;
-    v[0] += (double)ri * (double)(ri * m[i]);
+    v[0] += ri * (ri * m[i]);
   }
-  block_sum<1>(v);
-  if (!publish_partials<1>(v, partials, counter)) return;
+  double vb[1];
+  block_sum_widen<1>(v, vb);
+  if (!publish_partials<1>(vb, partials, counter)) return;
   double tot[1];
   gather_partials<1>(tot, partials, counter);
   if (threadIdx.x == 0) {

@@ -268,7 +268,7 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
   if (gate && *gate == 0) return;  // conditional product (mixed-precision replacement)
   constexpr int RPB = 256 / LANES;  // rows per block pass
   const int lane = threadIdx.x % LANES, sub = threadIdx.x / LANES;
-  double v[1] = {0.0};
+  T v[1] = {T(0)};  // this thread's share of (x, y), widened per warp
   for (int row0 = blockIdx.x * RPB; row0 < neq; row0 += gridDim.x * RPB) {
     const int row = row0 + sub;
     T acc0 = 0, acc1 = 0;
@@ -309,12 +309,13 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
       const T xi = x[row];
       const T yi = ad[row] * xi + s;
       y[row] = yi;
-      if (DOT) v[0] += (double)xi * (double)yi;
+      if (DOT) v[0] += xi * yi;
     }
   }
   if (!DOT) return;
-  block_sum<1>(v);
-  if (!publish_partials<1>(v, partials, counter)) return;
+  double vb[1];
+  block_sum_widen<1>(v, vb);
+  if (!publish_partials<1>(vb, partials, counter)) return;
   double tot[1];
   gather_partials<1>(tot, partials, counter);
   if (threadIdx.x == 0) {
@@ -343,7 +344,9 @@ void launch_gather(const CsrcDev &k, const T *al, const T *alt, const T *ad, con
                    const int32_t *gate = nullptr) {
   // 4 threads per row and 4 entries in flight per thread measured fastest on
   // the 64^3 HEXA8 cube (lanes 2/4/8 x unroll 2/4 swept: 166.8 us vs >= 174 us)
-  const int grid = gather_grid(k.neq, 4);
+  // a gated product (run only when *gate != 0) is launched with one wave of
+  // CTAs, so that it costs little when the gate is closed
+  const int grid = gate ? std::min(gather_grid(k.neq, 4), 1216) : gather_grid(k.neq, 4);
   if (k.ja16)
     gather_spmv_kernel<T, 4, 4, DOT, 0, true><<<grid, 256, 0, st>>>(
         k.neq, k.ia, k.ja, al, k.iat, k.jat, alt, ad, x, y, sc, partials, counter, gate, k.ja16,

@@ -170,7 +170,8 @@ int elx_set_matrix(elx_ctx *ctx, const double *ad, const double *al);
 
 /* Device-resident steps, no host copies: assembly from the resident u and b0
  * (elx_set_state), a solve from the resident b into the resident x, and
- * `reps` SpMVs y = K x on resident vectors.  All are stream-ordered on
+ * `reps` SpMVs y = K x on resident vectors, launched as the solvers launch
+ * them (with the fused dot product (x, y)).  All are stream-ordered on
  * elx_stream(ctx) and return once enqueued, except elx_solve_resident which
  * waits for convergence. */
 int elx_set_state(elx_ctx *ctx, const double *u, const double *b0);
