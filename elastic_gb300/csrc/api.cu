@@ -27,16 +27,22 @@ struct elx_ctx {
   // mesh (colour order) and structure
   DBuf conn, mat, elnum, slot, x, eq, e;
   DBuf ia, ja, iat, jat, pt, ja16, jat16;
+  // node blocks (when the numbering allows them): pattern and values
+  DBuf bia, bja, bt, bval, bval32;
+  bool use_blocks = false;
   // tiled transposed index of the SpMV and its halo slots
   DBuf tile_tgt, tile_out, tgt_col, tgt_start, tpos, halo_ptr, halo_slot, tile_desc, part;
   // matrix
   DBuf ad, al, alt, ad32, al32, alt32;
   int spmv_kind = elx::kSpmvGather;  // FP64 SpMV kernel family
   bool use_delta = true;             // 16-bit column deltas when the bandwidth fits
+  int gather_blocks = 0;             // gather SpMV grid (0: default)
   // state and solver vectors
   DBuf u, b0, b, xs, r, p, q, m, z;
   // mixed precision: FP32 inner PCG vectors and preconditioner
   DBuf m32, p32, q32, r32, x32;
+  // BiCGSTAB (r0, t) and GMRES (Krylov basis, small dense arrays, state)
+  DBuf r0v, tv, gbasis, garrays, gstate;
   // scalars, partials, counters, flags
   DBuf scal, partials, counters, flags, diag;
   elx::PcgScalars *h_scal = nullptr;  // pinned, 2 slots
@@ -47,6 +53,9 @@ struct elx_ctx {
 
   cudaGraphExec_t pcg_graph = nullptr;    // kBatch FP64 PCG iterations
   cudaGraphExec_t pcg32_graph = nullptr;  // kBatch FP32 inner PCG iterations
+  cudaGraphExec_t bicg_graph = nullptr;   // kBatch BiCGSTAB iterations
+  cudaGraphExec_t gmres_graph = nullptr;  // one GMRES(gmres_k) restart cycle
+  int gmres_k = 0, gmres_launches = 0;
   int pcg_graph_iters = 0;
   cudaEvent_t ev[2] = {nullptr, nullptr};
 
@@ -84,7 +93,10 @@ struct elx_ctx {
   void drop_graphs() {
     if (pcg_graph) cudaGraphExecDestroy(pcg_graph);
     if (pcg32_graph) cudaGraphExecDestroy(pcg32_graph);
-    pcg_graph = pcg32_graph = nullptr;
+    if (bicg_graph) cudaGraphExecDestroy(bicg_graph);
+    if (gmres_graph) cudaGraphExecDestroy(gmres_graph);
+    pcg_graph = pcg32_graph = bicg_graph = gmres_graph = nullptr;
+    gmres_k = gmres_launches = 0;
     pcg_graph_iters = 0;
   }
 
@@ -106,6 +118,12 @@ struct elx_ctx {
     k.jat16 = s.bw16 && use_delta ? jat16.as<uint16_t>() : nullptr;
     k.ad = ad.as<double>(); k.al = al.as<double>(); k.alt = alt.as<double>();
     k.ad32 = ad32.as<float>(); k.al32 = al32.as<float>(); k.alt32 = alt32.as<float>();
+    k.gather_blocks = gather_blocks;
+    if (use_blocks) {
+      k.bsize = s.bsize; k.nb = s.nb; k.nnzb = s.nnzb;
+      k.bia = bia.as<int32_t>(); k.bja = bja.as<int32_t>(); k.bt = bt.as<int32_t>();
+      k.bval = bval.as<double>(); k.bval32 = bval32.as<float>();
+    }
     return k;
   }
   elx::TileDev tile_dev() const {
@@ -199,36 +217,57 @@ void upload_structure(elx_ctx *c) {
   c->upload(c->e, m.e.data(), m.e.size());
   c->upload(c->ia, ia0.data(), ia0.size());
   c->upload(c->ja, ja0.data(), ja0.size());
-  choose_tiles(s);
-  elx::build_transpose(s);
-  c->upload(c->iat, s.iat.data(), s.iat.size());
-  c->upload(c->jat, s.jat.data(), s.jat.size());
-  c->upload(c->pt, s.pt.data(), s.pt.size());
-  if (s.bw16) {
-    c->upload(c->ja16, s.ja16.data(), s.ja16.size());
-    c->upload(c->jat16, s.jat16.data(), s.jat16.size());
-  } else {
-    c->release(c->ja16);
-    c->release(c->jat16);
-  }
   if (const char *env = getenv("ELX_DELTA16")) c->use_delta = atoi(env) != 0;
+  if (const char *env = getenv("ELX_GATHER_BLOCKS")) c->gather_blocks = atoi(env);
+  c->spmv_kind = elx::kSpmvGather;
   if (const char *env = getenv("ELX_SPMV"))
     c->spmv_kind = std::string(env) == "tile" ? elx::kSpmvTiled : elx::kSpmvGather;
-  c->upload(c->tile_tgt, s.tile_tgt.data(), s.tile_tgt.size());
-  c->upload(c->tile_out, s.tile_out.data(), s.tile_out.size());
-  c->upload(c->tgt_col, s.tgt_col.data(), s.tgt_col.size());
-  c->upload(c->tgt_start, s.tgt_start.data(), s.tgt_start.size());
-  c->upload(c->tpos, s.tpos.data(), s.tpos.size());
-  c->upload(c->halo_ptr, s.halo_ptr.data(), s.halo_ptr.size());
-  c->upload(c->halo_slot, s.halo_slot.data(), s.halo_slot.size());
-  c->upload(c->tile_desc, s.tile_desc.data(), s.tile_desc.size());
-  c->alloc(c->part, (size_t)s.tile_out[s.ntiles] * 8);
-  elx::prepare_tile_kernels(c->tile_dev());
+  // node blocks unless disabled (ELX_BLOCKS=0) or the tiled kernel is asked for
+  bool want_blocks = c->spmv_kind == elx::kSpmvGather;
+  if (const char *env = getenv("ELX_BLOCKS")) want_blocks = want_blocks && atoi(env) != 0;
+  if (want_blocks) elx::build_blocks(s, m.ndf);
+  c->use_blocks = want_blocks && s.blocked;
+  for (DBuf *v : {&c->iat, &c->jat, &c->pt, &c->ja16, &c->jat16, &c->tile_tgt, &c->tile_out,
+                  &c->tgt_col, &c->tgt_start, &c->tpos, &c->halo_ptr, &c->halo_slot,
+                  &c->tile_desc, &c->part, &c->alt, &c->bia, &c->bja, &c->bt, &c->bval,
+                  &c->bval32})
+    c->release(*v);
+  if (c->use_blocks) {
+    // the node-block product replaces both scalar kernel families
+    s.tile_rows = s.ntiles = 0;
+    s.bw16 = false;
+    c->upload(c->bia, s.bia.data(), s.bia.size());
+    c->upload(c->bja, s.bja.data(), s.bja.size());
+    c->upload(c->bt, s.bt.data(), s.bt.size());
+    c->alloc(c->bval, (size_t)s.nnzb * s.bsize * s.bsize * 8 + 64);
+    c->alloc(c->part, 16);
+  } else {
+    choose_tiles(s);
+    elx::build_transpose(s);
+    c->upload(c->iat, s.iat.data(), s.iat.size());
+    c->upload(c->jat, s.jat.data(), s.jat.size());
+    c->upload(c->pt, s.pt.data(), s.pt.size());
+    if (s.bw16) {
+      c->upload(c->ja16, s.ja16.data(), s.ja16.size());
+      c->upload(c->jat16, s.jat16.data(), s.jat16.size());
+    }
+    c->upload(c->tile_tgt, s.tile_tgt.data(), s.tile_tgt.size());
+    c->upload(c->tile_out, s.tile_out.data(), s.tile_out.size());
+    c->upload(c->tgt_col, s.tgt_col.data(), s.tgt_col.size());
+    c->upload(c->tgt_start, s.tgt_start.data(), s.tgt_start.size());
+    c->upload(c->tpos, s.tpos.data(), s.tpos.size());
+    c->upload(c->halo_ptr, s.halo_ptr.data(), s.halo_ptr.size());
+    c->upload(c->halo_slot, s.halo_slot.data(), s.halo_slot.size());
+    c->upload(c->tile_desc, s.tile_desc.data(), s.tile_desc.size());
+    c->alloc(c->part, (size_t)s.tile_out[s.ntiles] * 8);
+    elx::prepare_tile_kernels(c->tile_dev());
+    c->alloc(c->alt, (size_t)s.nad * 8 + 64);
+  }
   const size_t n = (size_t)s.neq, nad = (size_t)s.nad;
   c->alloc(c->ad, n * 8 + 64);
   c->alloc(c->al, nad * 8 + 64);
-  c->alloc(c->alt, nad * 8 + 64);
-  for (DBuf *v : {&c->ad32, &c->al32, &c->alt32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32})
+  for (DBuf *v : {&c->ad32, &c->al32, &c->alt32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32,
+                  &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate})
     c->release(*v);
   c->have_fp32 = false;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
@@ -255,17 +294,39 @@ void upload_structure(elx_ctx *c) {
 // vectors (once per structure), allocated on first use.
 void ensure_fp32(elx_ctx *c) {
   const size_t n = (size_t)c->s.neq, nad = (size_t)c->s.nad;
-  if (!c->ad32.p) {
-    c->alloc(c->ad32, n * 4 + 64);
-    c->alloc(c->al32, nad * 4 + 64);
-    c->alloc(c->alt32, nad * 4 + 64);
+  if (!c->m32.p) {
+    if (c->use_blocks) {
+      c->alloc(c->bval32, (size_t)c->s.nnzb * c->s.bsize * c->s.bsize * 4 + 64);
+    } else {
+      c->alloc(c->ad32, n * 4 + 64);
+      c->alloc(c->al32, nad * 4 + 64);
+      c->alloc(c->alt32, nad * 4 + 64);
+    }
     for (DBuf *v : {&c->m32, &c->p32, &c->q32, &c->r32, &c->x32}) c->alloc(*v, n * 4 + 64);
     c->drop_graphs();
   }
   if (c->have_fp32) return;
-  elx::launch_demote_values(c->csrc_dev(), c->stream);
-  c->launches += c->s.nad ? 2 : 1;
+  if (c->use_blocks) {
+    elx::launch_demote_blocks(c->csrc_dev(), c->stream);
+    c->launches += 1;
+  } else {
+    elx::launch_demote_values(c->csrc_dev(), c->stream);
+    c->launches += c->s.nad ? 2 : 1;
+  }
   c->have_fp32 = true;
+}
+
+// The kernel-side copies of a new CSRC matrix: the node blocks, or the
+// transposed upper values of the gather.
+void refresh_derived_values(elx_ctx *c) {
+  const elx::CsrcDev k = c->csrc_dev();
+  if (c->use_blocks) {
+    elx::launch_fill_blocks(k, c->stream);
+    c->launches += 2;
+  } else if (c->s.nad) {
+    elx::launch_transpose_values(k, c->stream);
+    c->launches += 1;
+  }
 }
 
 void assemble_resident(elx_ctx *c) {
@@ -282,8 +343,8 @@ void assemble_resident(elx_ctx *c) {
   const elx::CsrcDev k = c->csrc_dev();
   for (const elx::Segment &seg : s.segments)
     elx::launch_assembly(md, k, seg, c->u.as<double>(), c->b.as<double>(), bad, c->stream);
-  elx::launch_transpose_values(k, c->stream);
-  c->launches += (int64_t)s.segments.size() + (s.nad ? 1 : 0);
+  refresh_derived_values(c);
+  c->launches += (int64_t)s.segments.size();
   ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   c->sync();
   c->have_fp32 = false;
@@ -312,6 +373,7 @@ void build_preconditioner(elx_ctx *c) {
 }
 
 constexpr int kBatch = 16;        // PCG iterations per captured graph launch
+constexpr int kMaxGmresK = 256;   // GMRES restart length: one graph node per projection
 constexpr int kReplaceEvery = 4;  // mixed precision: replacement check interval
 
 // Captures kBatch iterations (FP64 or the FP32 inner iteration) as a graph.
@@ -510,11 +572,126 @@ void pcg_mixed(elx_ctx *c, double tol, int maxit, elx_info *info) {
                                  std::to_string(last.iters) + " iterations"};
 }
 
+// pbicgstab (Iters.f:1079-1349) on the device: right Jacobi, 2-norm test.
+void bicgstab64(elx_ctx *c, double tol, int maxit, elx_info *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  const size_t n = (size_t)c->s.neq;
+  if (!c->r0v.p) {
+    c->alloc(c->r0v, n * 8);
+    c->alloc(c->tv, n * 8);
+    c->drop_graphs();
+  }
+  build_preconditioner(c);
+  set_scalars(c, tol, maxit);
+  auto *sc = c->scal.as<elx::PcgScalars>();
+  elx::launch_bicg_start(c->s.neq, c->b.as<double>(), c->m.as<double>(), c->xs.as<double>(),
+                         c->r.as<double>(), c->r0v.as<double>(), c->p.as<double>(),
+                         c->z.as<double>(), sc, c->partials.as<double>(),
+                         c->counters.as<unsigned int>() + 2, c->stream);
+  c->launches += 1;
+  if (!c->bicg_graph) {
+    cudaGraph_t g;
+    ELX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (int i = 0; i < kBatch; i++)
+        elx::launch_bicg_iteration(c->csrc_dev(), c->m.as<double>(), c->xs.as<double>(),
+                                   c->r.as<double>(), c->r0v.as<double>(), c->p.as<double>(),
+                                   c->z.as<double>(), c->q.as<double>(), c->tv.as<double>(), sc,
+                                   c->partials.as<double>(), c->counters.as<unsigned int>() + 6,
+                                   c->stream);
+    } catch (...) {
+      cudaStreamEndCapture(c->stream, &g);
+      throw;
+    }
+    ELX_CUDA(cudaStreamEndCapture(c->stream, &g));
+    const cudaError_t inst = cudaGraphInstantiate(&c->bicg_graph, g, 0);
+    cudaGraphDestroy(g);
+    ELX_CUDA(inst);
+  }
+  elx::PcgScalars last = run_batches(c, c->bicg_graph, 5, maxit);
+  post_diagnostics(c);
+  const double secs =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (!last.done) last.status = ELX_ERR_NO_CONVERGENCE;
+  fill_info(c, info, last, secs);
+  if (info) info->mflops = 0.0;
+  if (last.status != ELX_OK)
+    throw Error{last.status, "BiCGSTAB: no convergence after " + std::to_string(last.iters) +
+                                 " iterations"};
+}
+
+// gmres (Iters.f:528-808) on the device: GMRES(k), left Jacobi, one captured
+// graph per restart cycle; maxit counts cycles, iters the Arnoldi steps.
+void gmres64(elx_ctx *c, int kdim, double tol, int maxit, elx_info *info) {
+  auto t0 = std::chrono::steady_clock::now();
+  require(kdim >= 1 && kdim <= kMaxGmresK, ELX_ERR_ARG, "GMRES restart length out of range");
+  const size_t n = (size_t)c->s.neq;
+  if (c->gmres_k != kdim || !c->gbasis.p) {
+    if (c->gmres_graph) cudaGraphExecDestroy(c->gmres_graph);
+    c->gmres_graph = nullptr;
+    c->alloc(c->gbasis, n * 8 * (size_t)(kdim + 1));
+    c->alloc(c->garrays, elx::gmres_array_doubles(kdim) * 8);
+    if (!c->gstate.p) c->alloc(c->gstate, sizeof(elx::GmresState));
+    c->gmres_k = kdim;
+  }
+  build_preconditioner(c);
+  auto *gs = c->gstate.as<elx::GmresState>();
+  elx::GmresState init{};
+  init.tol = tol;
+  init.maxit = maxit;
+  ELX_CUDA(cudaMemcpy(gs, &init, sizeof(init), cudaMemcpyHostToDevice));
+  ELX_CUDA(cudaMemsetAsync(c->garrays.p, 0, c->garrays.bytes, c->stream));
+  elx::launch_gmres_init(c->s.neq, c->b.as<double>(), c->m.as<double>(), c->xs.as<double>(),
+                         c->gbasis.as<double>(), gs, c->partials.as<double>(),
+                         c->counters.as<unsigned int>() + 2, c->stream);
+  c->launches += 1;
+  if (!c->gmres_graph) {
+    cudaGraph_t g;
+    ELX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      c->gmres_launches = elx::launch_gmres_cycle(
+          c->csrc_dev(), kdim, c->b.as<double>(), c->m.as<double>(), c->xs.as<double>(),
+          c->gbasis.as<double>(), gs, c->garrays.as<double>(), c->partials.as<double>(),
+          c->counters.as<unsigned int>() + 6, c->stream);
+    } catch (...) {
+      cudaStreamEndCapture(c->stream, &g);
+      throw;
+    }
+    ELX_CUDA(cudaStreamEndCapture(c->stream, &g));
+    const cudaError_t inst = cudaGraphInstantiate(&c->gmres_graph, g, 0);
+    cudaGraphDestroy(g);
+    ELX_CUDA(inst);
+  }
+  elx::GmresState st{};
+  for (int cyc = 0; cyc <= maxit; cyc++) {
+    ELX_CUDA(cudaMemcpyAsync(&st, gs, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
+    c->sync();
+    if (!st.live) break;
+    ELX_CUDA(cudaGraphLaunch(c->gmres_graph, c->stream));
+    c->launches += c->gmres_launches;
+  }
+  ELX_CUDA(cudaMemcpyAsync(&st, gs, sizeof(st), cudaMemcpyDeviceToHost, c->stream));
+  post_diagnostics(c);
+  const double secs =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  elx::PcgScalars last{};
+  last.iters = st.nit;
+  last.status = st.done ? st.status : ELX_ERR_NO_CONVERGENCE;
+  last.conv = st.econv;
+  fill_info(c, info, last, secs);
+  if (info) {
+    info->mflops = 0.0;
+    info->refinements = st.cycles;  // restart cycles
+  }
+  if (last.status != ELX_OK)
+    throw Error{last.status, "GMRES: no convergence after " + std::to_string(st.cycles) +
+                                 " cycles (" + std::to_string(st.nit) + " iterations)"};
+}
+
 void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit, int ngram,
                     elx_info *info) {
   require(c->have_matrix, ELX_ERR_STATE, "solve before the matrix is assembled");
   require(tol > 0 && maxit >= 0, ELX_ERR_ARG, "tol must be > 0 and maxit >= 0");
-  (void)ngram;
   if (info) std::memset(info, 0, sizeof(*info));
   if (solver == ELX_SOLVER_PCG && precision == ELX_PREC_FP64) {
     pcg64(c, tol, maxit, info);
@@ -522,6 +699,14 @@ void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit
   }
   if (solver == ELX_SOLVER_PCG && precision == ELX_PREC_MIXED) {
     pcg_mixed(c, tol, maxit, info);
+    return;
+  }
+  if (solver == ELX_SOLVER_BICGSTAB && precision == ELX_PREC_FP64) {
+    bicgstab64(c, tol, maxit, info);
+    return;
+  }
+  if (solver == ELX_SOLVER_GMRES && precision == ELX_PREC_FP64) {
+    gmres64(c, ngram, tol, maxit, info);
     return;
   }
   throw Error{ELX_ERR_ARG, "solver/precision combination not available"};
@@ -627,7 +812,9 @@ void elx_destroy(elx_ctx *c) {
                   &c->iat, &c->jat, &c->pt, &c->ja16, &c->jat16, &c->alt, &c->alt32,
                   &c->tile_tgt, &c->tile_out, &c->tgt_col, &c->tgt_start, &c->tpos,
                   &c->halo_ptr, &c->halo_slot, &c->tile_desc, &c->part, &c->ad, &c->al,
-                  &c->ad32, &c->al32,
+                  &c->ad32, &c->al32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32,
+                  &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate,
+                  &c->bia, &c->bja, &c->bt, &c->bval, &c->bval32,
                   &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
                   &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
     c->release(*d);
@@ -818,8 +1005,7 @@ int elx_set_matrix(elx_ctx *c, const double *ad, const double *al) {
     if (c->s.nad)
       ELX_CUDA(cudaMemcpyAsync(c->al.p, al, (size_t)c->s.nad * 8, cudaMemcpyHostToDevice,
                                c->stream));
-    elx::launch_transpose_values(c->csrc_dev(), c->stream);
-    c->launches += c->s.nad ? 1 : 0;
+    refresh_derived_values(c);
     c->sync();
     c->have_matrix = true;
     c->have_fp32 = false;

@@ -1,0 +1,246 @@
+// Node-block (BCSR) form of the CSRC matrix and its product y = K x.
+//
+// The elasticity matrix is a matrix of B x B node blocks (B = ndf): when no
+// node is only partly fixed, numeq's numbering (Numeq.f:139-192) puts the B
+// dofs of a node on consecutive equations, so block row I is equations
+// B I .. B I + B - 1.  The CSRC arrays (ad, al: the reference's layout, which
+// the assembly fills and the C ABI returns) are expanded after each assembly
+// into full block rows -- lower blocks, the diagonal block, upper blocks as
+// transposed copies of the lower ones -- with one column index per block
+// instead of one per entry:
+//
+//   * bytes per stored entry: B^2 values + 1 index per B^2 entries, so
+//     4.4 B (FP32) / 8.4 B (FP64) per entry against 6 / 10 B for the
+//     two-sided gather with 16-bit column deltas;
+//   * one thread per matrix row walks its block row: per block one column
+//     index and B values, B x values, B FMAs -- every FMA lane does useful
+//     work (no partially filled lane groups), which is what bounds the FP64
+//     product on this GPU (its FP64 pipe retires 2 FMAs per clock per SM);
+//   * no reductions inside a row, so the FP64 pipe does nothing but the
+//     product's own FMAs.
+//
+// The product is still the reference's y = D x + L x + L^T x (matvec_csrcsym1,
+// Matvec.f:528-621) with the same values, summed in a different order.
+#include <algorithm>
+
+#include "elx_krylov.h"
+#include "elx_reduce.cuh"
+
+namespace elx {
+namespace {
+
+// Lower and diagonal blocks from the CSRC arrays: lower block q of block row
+// I holds, in row B I + a, the B consecutive entries al[ia[B I + a] + B q ..];
+// the diagonal block's strict lower part is the last a entries of row B I + a.
+template <int B>
+__global__ void fill_lower_blocks_kernel(int64_t nnzb, const int32_t *__restrict__ bia,
+                                         const int32_t *__restrict__ bt,
+                                         const int32_t *__restrict__ ia,
+                                         const double *__restrict__ ad,
+                                         const double *__restrict__ al,
+                                         double *__restrict__ bval) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnzb;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t t = bt[p];
+    if (t >= 0) continue;
+    const int I = -1 - t;
+    const int r0 = B * I;
+    const int nl = (ia[r0 + 1] - ia[r0]) / B;
+    const int q = (int)(p - bia[I]);
+    double *out = bval + p * (B * B);
+    if (q < nl) {
+#pragma unroll
+      for (int a = 0; a < B; a++)
+#pragma unroll
+        for (int b = 0; b < B; b++) out[a * B + b] = al[ia[r0 + a] + B * q + b];
+    } else {
+#pragma unroll
+      for (int a = 0; a < B; a++)
+#pragma unroll
+        for (int b = 0; b < B; b++)
+          out[a * B + b] = a == b  ? ad[r0 + a]
+                           : a > b ? al[ia[r0 + a] + B * nl + b]
+                                   : al[ia[r0 + b] + B * nl + a];
+    }
+  }
+}
+
+// Upper blocks: the transpose of their mirror.
+template <int B>
+__global__ void fill_upper_blocks_kernel(int64_t nnzb, const int32_t *__restrict__ bt,
+                                         double *__restrict__ bval) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < nnzb;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t t = bt[p];
+    if (t < 0) continue;
+    const double *src = bval + (int64_t)t * (B * B);
+    double *out = bval + p * (B * B);
+#pragma unroll
+    for (int a = 0; a < B; a++)
+#pragma unroll
+      for (int b = 0; b < B; b++) out[a * B + b] = src[b * B + a];
+  }
+}
+
+__global__ void demote_blocks_kernel(int64_t n, const double *__restrict__ src,
+                                     float *__restrict__ dst) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+// y = K x, one thread per row, U blocks in flight, then the GatherEpi
+// epilogue (dot products reduced in a fixed order over a fixed grid).
+template <class T, int B, int EPI, int U>
+__global__ void __launch_bounds__(256)
+bcsr_spmv_kernel(int neq, const int32_t *__restrict__ bia, const int32_t *__restrict__ bja,
+                 const T *__restrict__ bval, const T *__restrict__ x, T *__restrict__ y,
+                 const T *__restrict__ w, PcgScalars *sc, double *partials,
+                 unsigned int *counter, const int32_t *gate) {
+  constexpr bool DOT = EPI == kEpiPcg || EPI == kEpiBicgAlpha || EPI == kEpiBicgOmega;
+  constexpr int NV = EPI == kEpiBicgOmega ? 2 : 1;
+  constexpr int BB = B * B;
+  if (DOT && sc->done) return;
+  if (gate && *gate == 0) return;
+  T v[NV];
+#pragma unroll
+  for (int c = 0; c < NV; c++) v[c] = T(0);
+  for (int row = blockIdx.x * 256 + threadIdx.x; row < neq; row += gridDim.x * 256) {
+    const int I = row / B, a = row - I * B;
+    const int pb = bia[I], pe = bia[I + 1];
+    const T *vr = bval + (size_t)pb * BB + a * B;
+    T acc0 = 0, acc1 = 0;
+    int p = pb;
+    for (; p + U <= pe; p += U) {
+      int J[U];
+      T av[U][B], xv[U][B];
+#pragma unroll
+      for (int u = 0; u < U; u++) J[u] = bja[p + u];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int b = 0; b < B; b++) av[u][b] = vr[(size_t)(p - pb + u) * BB + b];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int b = 0; b < B; b++) xv[u][b] = x[J[u] * B + b];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int b = 0; b < B; b++) {
+          if (u & 1)
+            acc1 += av[u][b] * xv[u][b];
+          else
+            acc0 += av[u][b] * xv[u][b];
+        }
+    }
+    for (; p < pe; p++) {
+      const int J = bja[p];
+#pragma unroll
+      for (int b = 0; b < B; b++) acc0 += vr[(size_t)(p - pb) * BB + b] * x[J * B + b];
+    }
+    T yi = acc0 + acc1;
+    if (EPI == kEpiScale) yi = yi * w[row];
+    y[row] = yi;
+    if (EPI == kEpiPcg) v[0] += x[row] * yi;
+    if (EPI == kEpiBicgAlpha) v[0] += yi * w[row];
+    if (EPI == kEpiBicgOmega) {
+      v[0] += yi * w[row];
+      v[1] += yi * yi;
+    }
+  }
+  if (!DOT) return;
+  double vb[NV];
+  block_sum_widen<NV>(v, vb);
+  if (!publish_partials<NV>(vb, partials, counter)) return;
+  double tot[NV];
+  gather_partials<NV>(tot, partials, counter);
+  if (threadIdx.x == 0) {
+    if (EPI == kEpiPcg) {
+      sc->pq = tot[0];
+      sc->alpha = sc->d / tot[0];
+    } else if (EPI == kEpiBicgAlpha) {
+      sc->pq = tot[0];
+      sc->alpha = sc->rho / tot[0];
+      sc->iters += 1;
+    } else if (EPI == kEpiBicgOmega) {
+      sc->omega = tot[0] / tot[NV - 1];
+    }
+  }
+}
+
+int fill_grid(int64_t n) {
+  const int64_t g = (n + 255) / 256;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
+}
+
+}  // namespace
+
+void launch_fill_blocks(const CsrcDev &k, cudaStream_t st) {
+  if (!k.bval || k.nnzb == 0) return;
+  const int g = fill_grid(k.nnzb);
+  if (k.bsize == 3) {
+    fill_lower_blocks_kernel<3><<<g, 256, 0, st>>>(k.nnzb, k.bia, k.bt, k.ia, k.ad, k.al, k.bval);
+    fill_upper_blocks_kernel<3><<<g, 256, 0, st>>>(k.nnzb, k.bt, k.bval);
+  } else {
+    fill_lower_blocks_kernel<2><<<g, 256, 0, st>>>(k.nnzb, k.bia, k.bt, k.ia, k.ad, k.al, k.bval);
+    fill_upper_blocks_kernel<2><<<g, 256, 0, st>>>(k.nnzb, k.bt, k.bval);
+  }
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_demote_blocks(const CsrcDev &k, cudaStream_t st) {
+  if (!k.bval || !k.bval32 || k.nnzb == 0) return;
+  const int64_t n = k.nnzb * k.bsize * k.bsize;
+  demote_blocks_kernel<<<fill_grid(n), 256, 0, st>>>(n, k.bval, k.bval32);
+  ELX_CUDA(cudaGetLastError());
+}
+
+// The gather entry points route here when the matrix has node blocks.
+template <class T, int EPI>
+void launch_bcsr(const CsrcDev &k, const T *x, T *y, const T *w, PcgScalars *sc,
+                 double *partials, unsigned int *counter, const int32_t *gate,
+                 cudaStream_t st) {
+  const T *val;
+  if constexpr (sizeof(T) == 8)
+    val = k.bval;
+  else
+    val = k.bval32;
+  ELX_REQUIRE(val != nullptr, ELX_ERR_STATE, "node-block values missing");
+  // one wave of 8 CTAs per SM (152 SMs): 134 us against 142 us for one CTA
+  // per 256 rows on the 64^3 HEXA8 cube (FP64), 47.6 against 52.0 us on the
+  // 48^3 TETRA4 mesh
+  int grid = std::max(1, std::min((k.neq + 255) / 256, 1216));
+  if (k.gather_blocks > 0) grid = std::min((k.neq + 255) / 256, k.gather_blocks);
+  if (k.bsize == 3)
+    bcsr_spmv_kernel<T, 3, EPI, 3><<<grid, 256, 0, st>>>(k.neq, k.bia, k.bja, val, x, y, w, sc,
+                                                         partials, counter, gate);
+  else
+    bcsr_spmv_kernel<T, 2, EPI, 4><<<grid, 256, 0, st>>>(k.neq, k.bia, k.bja, val, x, y, w, sc,
+                                                         partials, counter, gate);
+  ELX_CUDA(cudaGetLastError());
+}
+
+template void launch_bcsr<double, kEpiNone>(const CsrcDev &, const double *, double *,
+                                            const double *, PcgScalars *, double *,
+                                            unsigned int *, const int32_t *, cudaStream_t);
+template void launch_bcsr<double, kEpiPcg>(const CsrcDev &, const double *, double *,
+                                           const double *, PcgScalars *, double *,
+                                           unsigned int *, const int32_t *, cudaStream_t);
+template void launch_bcsr<double, kEpiBicgAlpha>(const CsrcDev &, const double *, double *,
+                                                 const double *, PcgScalars *, double *,
+                                                 unsigned int *, const int32_t *, cudaStream_t);
+template void launch_bcsr<double, kEpiBicgOmega>(const CsrcDev &, const double *, double *,
+                                                 const double *, PcgScalars *, double *,
+                                                 unsigned int *, const int32_t *, cudaStream_t);
+template void launch_bcsr<double, kEpiScale>(const CsrcDev &, const double *, double *,
+                                             const double *, PcgScalars *, double *,
+                                             unsigned int *, const int32_t *, cudaStream_t);
+template void launch_bcsr<float, kEpiNone>(const CsrcDev &, const float *, float *,
+                                           const float *, PcgScalars *, double *,
+                                           unsigned int *, const int32_t *, cudaStream_t);
+template void launch_bcsr<float, kEpiPcg>(const CsrcDev &, const float *, float *, const float *,
+                                          PcgScalars *, double *, unsigned int *,
+                                          const int32_t *, cudaStream_t);
+
+}  // namespace elx

@@ -103,6 +103,16 @@ struct Structure {
   // used when the matrix bandwidth fits (bw16 = true)
   bool bw16 = false;
   std::vector<uint16_t> ja16, jat16;
+  // Node blocks (BCSR): when the equations come in runs of B = ndf per node
+  // (every node all free or all fixed), K is a matrix of B x B node blocks.
+  // Block row I holds equations B I .. B I + B - 1; its blocks in ascending
+  // block column: the lower blocks (the order of the CSRC row B I), the
+  // diagonal block, the upper blocks.  bt: for an upper block the position
+  // of its mirror (a lower block), for a lower or diagonal block -1 - I.
+  bool blocked = false;
+  int32_t bsize = 0, nb = 0;
+  int64_t nnzb = 0;
+  std::vector<int32_t> bia, bja, bt;
 };
 
 // host structure routines (structure.cpp)
@@ -117,6 +127,7 @@ void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> 
 void derive_structure(const Mesh &m, Structure &s);
 void build_tiles(Structure &s, int tile_rows);
 void build_transpose(Structure &s);
+void build_blocks(Structure &s, int bsize);
 
 // ------------------------------------------------------------- kernels
 struct MeshDev {
@@ -142,6 +153,13 @@ struct CsrcDev {
   const uint16_t *ja16, *jat16;  // 16-bit column deltas (null: use ja/jat)
   double *ad, *al, *alt;
   float *ad32, *al32, *alt32;
+  int32_t gather_blocks = 0;  // grid of the gather SpMV (0: default)
+  // node blocks (null bval: none); see Structure
+  int32_t bsize = 0, nb = 0;
+  int64_t nnzb = 0;
+  const int32_t *bia = nullptr, *bja = nullptr, *bt = nullptr;
+  double *bval = nullptr;
+  float *bval32 = nullptr;
 };
 
 struct TileDev {
@@ -167,6 +185,9 @@ void launch_tile_spmv32(const CsrcDev &k, const TileDev &t, const float *x, floa
                         float *part, int32_t *err, cudaStream_t st);
 void launch_demote_values(const CsrcDev &k, cudaStream_t st);
 void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
+// Node-block values from the CSRC arrays (k.bval), and their FP32 copy.
+void launch_fill_blocks(const CsrcDev &k, cudaStream_t st);
+void launch_demote_blocks(const CsrcDev &k, cudaStream_t st);
 // Two-sided gather SpMV: y = K x reading the lower part (ja, al) and the
 // upper part through the transposed copy (jat, alt); with sc != nullptr it
 // also forms (x, y) and alpha = d / (x, y).
@@ -175,5 +196,21 @@ void launch_gather_spmv64(const CsrcDev &k, const double *x, double *y, PcgScala
                           const int32_t *gate = nullptr);
 void launch_gather_spmv32(const CsrcDev &k, const float *x, float *y, PcgScalars *sc,
                           double *partials, unsigned int *counter, cudaStream_t st);
+
+// Epilogues of the gather SpMV: what it does with y = K x besides storing it.
+enum GatherEpi : int {
+  kEpiNone = 0,       // nothing
+  kEpiPcg = 1,        // pq = (x, y), alpha = d / pq
+  kEpiBicgAlpha = 2,  // pq = (w, y), alpha = rho / pq, iters += 1   (w = r0)
+  kEpiBicgOmega = 3,  // omega = (w, y) / (y, y)                      (w = r)
+  kEpiScale = 4,      // y = w .* (K x), no dot                       (w = M)
+};
+void launch_gather_epi64(const CsrcDev &k, int epi, const double *x, double *y, const double *w,
+                         PcgScalars *sc, double *partials, unsigned int *counter,
+                         const int32_t *gate, cudaStream_t st);
+// The node-block product (bcsr.cu), with the same epilogues.
+template <class T, int EPI>
+void launch_bcsr(const CsrcDev &k, const T *x, T *y, const T *w, PcgScalars *sc,
+                 double *partials, unsigned int *counter, const int32_t *gate, cudaStream_t st);
 
 }  // namespace elx

@@ -14,12 +14,30 @@ struct PcgScalars {
   double alpha, beta, pq;
   double rmax;    // mixed precision: ||r||_M at the last residual replacement
   double delta;   // mixed precision: replace when ||r||_M < delta * rmax (input)
+  double rho;     // BiCGSTAB: (r, r0)
+  double omega;   // BiCGSTAB: (t, r) / (t, t)
   int32_t maxit;  // (input)
   int32_t iters;
   int32_t done;
   int32_t status;
   int32_t update;    // mixed precision: a residual replacement is due
   int32_t nupdates;  // mixed precision: replacements so far
+};
+
+// State of one GMRES(k) solve, resident in device memory (the small dense
+// arrays live in a separate buffer of gmres_array_doubles(k) doubles).
+struct GmresState {
+  double tol;         // (input)
+  double econv;       // tol ||M b||
+  int32_t maxit;      // restart cycles (input)
+  int32_t live;       // the solve is running
+  int32_t run;        // the current cycle's Arnoldi loop is running
+  int32_t ni;         // Arnoldi steps in the current cycle
+  int32_t nit;        // Arnoldi steps in all cycles
+  int32_t cycles;
+  int32_t conv_flag;  // |e(ni+1)| <= econv after the current cycle
+  int32_t done;
+  int32_t status;
 };
 
 int vector_grid(int n);
@@ -56,6 +74,22 @@ void launch_rel_iteration(const CsrcDev &k, const double *b, const double *m, do
                           const float *m32, PcgScalars *sc, double *partials,
                           unsigned int *counters, bool replacement_point, cudaStream_t st);
 void launch_convert(int n, const double *src, float *dst, cudaStream_t st);
+
+// BiCGSTAB and GMRES (krylov_ns.cu)
+void launch_bicg_start(int n, const double *b, const double *m, double *x, double *r,
+                       double *r0, double *p, double *z, PcgScalars *sc, double *partials,
+                       unsigned int *counter, cudaStream_t st);
+void launch_bicg_iteration(const CsrcDev &k, const double *m, double *x, double *r,
+                           const double *r0, double *p, double *z, double *v, double *t,
+                           PcgScalars *sc, double *partials, unsigned int *counters,
+                           cudaStream_t st);
+size_t gmres_array_doubles(int k);
+void launch_gmres_init(int n, const double *b, const double *m, double *x, double *g1,
+                       GmresState *gs, double *partials, unsigned int *counter,
+                       cudaStream_t st);
+int launch_gmres_cycle(const CsrcDev &k, int kdim, const double *b, const double *m, double *x,
+                       double *g, GmresState *gs, double *arrays, double *partials,
+                       unsigned int *counter, cudaStream_t st);
 void launch_widen(int n, const float *src, double *dst, cudaStream_t st);
 
 }  // namespace elx

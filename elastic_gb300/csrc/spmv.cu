@@ -249,26 +249,33 @@ spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32
 // Two-sided gather: LANES threads per row stride over the row's lower
 // entries and over its upper entries (column i of L through the transposed
 // copy), UNROLL entries in flight per thread, then a fixed shuffle tree.
-// Rows are walked with a fixed grid so that the optional dot (x, y) reduces
-// in a fixed order.
+// Rows are walked with a fixed grid so that the epilogue's dot products
+// reduce in a fixed order.
 // BASE is the index base of ia/ja/iat/jat contents (0 inside the library,
 // 1 for arrays in the reference's 1-based convention).  With DELTA the
 // columns come as 16-bit distances from the row (ja16: row - col below the
 // diagonal, jat16: col - row above it): 2 bytes per stored entry instead of 4.
-template <class T, int LANES, int U, bool DOT, int BASE = 0, bool DELTA = false>
+// EPI selects what happens besides y = K x (GatherEpi); w is the epilogue's
+// second vector.  A launch with gate != nullptr runs only while *gate != 0.
+template <class T, int LANES, int U, int EPI, int BASE = 0, bool DELTA = false>
 __global__ void __launch_bounds__(256)
 gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__restrict__ ja,
                    const T *__restrict__ al, const int32_t *__restrict__ iat,
                    const int32_t *__restrict__ jat, const T *__restrict__ alt,
                    const T *__restrict__ ad, const T *__restrict__ x, T *__restrict__ y,
-                   PcgScalars *sc, double *partials, unsigned int *counter,
-                   const int32_t *gate, const uint16_t *__restrict__ ja16 = nullptr,
+                   const T *__restrict__ w, PcgScalars *sc, double *partials,
+                   unsigned int *counter, const int32_t *gate,
+                   const uint16_t *__restrict__ ja16 = nullptr,
                    const uint16_t *__restrict__ jat16 = nullptr) {
+  constexpr bool DOT = EPI == kEpiPcg || EPI == kEpiBicgAlpha || EPI == kEpiBicgOmega;
+  constexpr int NV = EPI == kEpiBicgOmega ? 2 : 1;
   if (DOT && sc->done) return;
-  if (gate && *gate == 0) return;  // conditional product (mixed-precision replacement)
+  if (gate && *gate == 0) return;
   constexpr int RPB = 256 / LANES;  // rows per block pass
   const int lane = threadIdx.x % LANES, sub = threadIdx.x / LANES;
-  T v[1] = {T(0)};  // this thread's share of (x, y), widened per warp
+  T v[NV];  // this thread's share of the dot products, widened per warp
+#pragma unroll
+  for (int c = 0; c < NV; c++) v[c] = T(0);
   for (int row0 = blockIdx.x * RPB; row0 < neq; row0 += gridDim.x * RPB) {
     const int row = row0 + sub;
     T acc0 = 0, acc1 = 0;
@@ -307,20 +314,34 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
     for (int off = LANES / 2; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off, LANES);
     if (row < neq && lane == 0) {
       const T xi = x[row];
-      const T yi = ad[row] * xi + s;
+      T yi = ad[row] * xi + s;
+      if (EPI == kEpiScale) yi = yi * w[row];
       y[row] = yi;
-      if (DOT) v[0] += xi * yi;
+      if (EPI == kEpiPcg) v[0] += xi * yi;
+      if (EPI == kEpiBicgAlpha) v[0] += yi * w[row];
+      if (EPI == kEpiBicgOmega) {
+        v[0] += yi * w[row];
+        v[1] += yi * yi;
+      }
     }
   }
   if (!DOT) return;
-  double vb[1];
-  block_sum_widen<1>(v, vb);
-  if (!publish_partials<1>(vb, partials, counter)) return;
-  double tot[1];
-  gather_partials<1>(tot, partials, counter);
+  double vb[NV];
+  block_sum_widen<NV>(v, vb);
+  if (!publish_partials<NV>(vb, partials, counter)) return;
+  double tot[NV];
+  gather_partials<NV>(tot, partials, counter);
   if (threadIdx.x == 0) {
-    sc->pq = tot[0];
-    sc->alpha = sc->d / tot[0];
+    if (EPI == kEpiPcg) {
+      sc->pq = tot[0];
+      sc->alpha = sc->d / tot[0];
+    } else if (EPI == kEpiBicgAlpha) {
+      sc->pq = tot[0];
+      sc->alpha = sc->rho / tot[0];
+      sc->iters += 1;
+    } else if (EPI == kEpiBicgOmega) {
+      sc->omega = tot[0] / tot[NV - 1];
+    }
   }
 }
 
@@ -338,23 +359,29 @@ int gather_grid(int neq, int lanes) {
   return g < 4864 ? (g < 1 ? 1 : g) : 4864;  // fixed upper bound: 152 SMs x 32
 }
 
-template <class T, bool DOT>
+template <class T, int EPI>
 void launch_gather(const CsrcDev &k, const T *al, const T *alt, const T *ad, const T *x, T *y,
-                   PcgScalars *sc, double *partials, unsigned int *counter, cudaStream_t st,
-                   const int32_t *gate = nullptr) {
+                   const T *w, PcgScalars *sc, double *partials, unsigned int *counter,
+                   cudaStream_t st, const int32_t *gate = nullptr) {
+  if (k.bval) {  // node blocks
+    launch_bcsr<T, EPI>(k, x, y, w, sc, partials, counter, gate, st);
+    return;
+  }
   // 4 threads per row and 4 entries in flight per thread measured fastest on
   // the 64^3 HEXA8 cube (lanes 2/4/8 x unroll 2/4 swept: 166.8 us vs >= 174 us)
   // a gated product (run only when *gate != 0) is launched with one wave of
   // CTAs, so that it costs little when the gate is closed
-  const int grid = gate ? std::min(gather_grid(k.neq, 4), 1216) : gather_grid(k.neq, 4);
+  int grid = gather_grid(k.neq, 4);
+  if (k.gather_blocks > 0) grid = std::min(grid, k.gather_blocks);
+  if (gate) grid = std::min(grid, 1216);
   if (k.ja16)
-    gather_spmv_kernel<T, 4, 4, DOT, 0, true><<<grid, 256, 0, st>>>(
-        k.neq, k.ia, k.ja, al, k.iat, k.jat, alt, ad, x, y, sc, partials, counter, gate, k.ja16,
-        k.jat16);
+    gather_spmv_kernel<T, 4, 4, EPI, 0, true><<<grid, 256, 0, st>>>(
+        k.neq, k.ia, k.ja, al, k.iat, k.jat, alt, ad, x, y, w, sc, partials, counter, gate,
+        k.ja16, k.jat16);
   else
-    gather_spmv_kernel<T, 4, 4, DOT><<<grid, 256, 0, st>>>(k.neq, k.ia, k.ja, al, k.iat, k.jat,
-                                                           alt, ad, x, y, sc, partials, counter,
-                                                           gate);
+    gather_spmv_kernel<T, 4, 4, EPI><<<grid, 256, 0, st>>>(k.neq, k.ia, k.ja, al, k.iat, k.jat,
+                                                           alt, ad, x, y, w, sc, partials,
+                                                           counter, gate);
   ELX_CUDA(cudaGetLastError());
 }
 
@@ -435,18 +462,50 @@ void launch_gather_spmv64(const CsrcDev &k, const double *x, double *y, PcgScala
                           double *partials, unsigned int *counter, cudaStream_t st,
                           const int32_t *gate) {
   if (sc)
-    launch_gather<double, true>(k, k.al, k.alt, k.ad, x, y, sc, partials, counter, st, gate);
+    launch_gather<double, kEpiPcg>(k, k.al, k.alt, k.ad, x, y, nullptr, sc, partials, counter,
+                                   st, gate);
   else
-    launch_gather<double, false>(k, k.al, k.alt, k.ad, x, y, nullptr, nullptr, nullptr, st,
-                                 gate);
+    launch_gather<double, kEpiNone>(k, k.al, k.alt, k.ad, x, y, nullptr, nullptr, nullptr,
+                                    nullptr, st, gate);
 }
 
 void launch_gather_spmv32(const CsrcDev &k, const float *x, float *y, PcgScalars *sc,
                           double *partials, unsigned int *counter, cudaStream_t st) {
   if (sc)
-    launch_gather<float, true>(k, k.al32, k.alt32, k.ad32, x, y, sc, partials, counter, st);
+    launch_gather<float, kEpiPcg>(k, k.al32, k.alt32, k.ad32, x, y, nullptr, sc, partials,
+                                  counter, st);
   else
-    launch_gather<float, false>(k, k.al32, k.alt32, k.ad32, x, y, nullptr, nullptr, nullptr, st);
+    launch_gather<float, kEpiNone>(k, k.al32, k.alt32, k.ad32, x, y, nullptr, nullptr, nullptr,
+                                   nullptr, st);
+}
+
+void launch_gather_epi64(const CsrcDev &k, int epi, const double *x, double *y, const double *w,
+                         PcgScalars *sc, double *partials, unsigned int *counter,
+                         const int32_t *gate, cudaStream_t st) {
+  switch (epi) {
+    case kEpiNone:
+      launch_gather<double, kEpiNone>(k, k.al, k.alt, k.ad, x, y, w, sc, partials, counter, st,
+                                      gate);
+      break;
+    case kEpiPcg:
+      launch_gather<double, kEpiPcg>(k, k.al, k.alt, k.ad, x, y, w, sc, partials, counter, st,
+                                     gate);
+      break;
+    case kEpiBicgAlpha:
+      launch_gather<double, kEpiBicgAlpha>(k, k.al, k.alt, k.ad, x, y, w, sc, partials, counter,
+                                           st, gate);
+      break;
+    case kEpiBicgOmega:
+      launch_gather<double, kEpiBicgOmega>(k, k.al, k.alt, k.ad, x, y, w, sc, partials, counter,
+                                           st, gate);
+      break;
+    case kEpiScale:
+      launch_gather<double, kEpiScale>(k, k.al, k.alt, k.ad, x, y, w, sc, partials, counter, st,
+                                       gate);
+      break;
+    default:
+      throw Error{ELX_ERR_ARG, "unknown SpMV epilogue"};
+  }
 }
 
 }  // namespace elx
@@ -507,9 +566,9 @@ extern "C" int elx_spmv_dot_noalloc(int32_t neq, const int32_t *ia, const int32_
       cudaSuccess)
     return ELX_ERR_CUDA;
   const int grid = (neq + kNoAllocRowsPerBlock - 1) / kNoAllocRowsPerBlock;
-  gather_spmv_kernel<double, 4, 4, true, 1><<<grid, 256, 0, st>>>(
-      neq, ia, ja, al, iat, jat, alt, ad, x, y, &sc->scalars, sc->partials, &sc->counter,
-      nullptr);
+  gather_spmv_kernel<double, 4, 4, kEpiPcg, 1><<<grid, 256, 0, st>>>(
+      neq, ia, ja, al, iat, jat, alt, ad, x, y, nullptr, &sc->scalars, sc->partials,
+      &sc->counter, nullptr);
   if (cudaGetLastError() != cudaSuccess) return ELX_ERR_CUDA;
   if (cudaMemcpyAsync(xy, &sc->scalars.pq, sizeof(double), cudaMemcpyDeviceToDevice, st) !=
       cudaSuccess)

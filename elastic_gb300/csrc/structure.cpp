@@ -522,4 +522,73 @@ void build_transpose(Structure &s) {
   }
 }
 
+// Node blocks of the CSRC pattern.  numeq (Numeq.f:139-192) numbers the free
+// dofs of each node consecutively in node order, so when no node is only
+// partly fixed, equation B I + a is dof a of the I-th free node and the
+// lower pattern of row B I + a is: B consecutive columns per lower neighbour
+// node J (ascending), then the a columns B I .. B I + a - 1 of the node's own
+// block.  Checks exactly that shape; any other pattern leaves s.blocked false
+// (the scalar kernels then handle the matrix).
+void build_blocks(Structure &s, int bsize) {
+  s.blocked = false;
+  s.bsize = s.nb = 0;
+  s.nnzb = 0;
+  s.bia.clear();
+  s.bja.clear();
+  s.bt.clear();
+  const int B = bsize;
+  if (B < 2 || B > 3 || s.neq % B) return;
+  const int nb = s.neq / B;
+  std::vector<int32_t> nl(nb), nup(nb, 0);
+  for (int I = 0; I < nb; I++) {
+    const int r0 = B * I;
+    const int32_t k0 = s.ia[r0] - 1;
+    const int32_t len0 = s.ia[r0 + 1] - s.ia[r0];
+    if (len0 % B) return;
+    const int n = len0 / B;
+    nl[I] = n;
+    for (int a = 0; a < B; a++) {
+      const int r = r0 + a;
+      const int32_t k = s.ia[r] - 1;
+      if (s.ia[r + 1] - s.ia[r] != B * n + a) return;
+      for (int q = 0; q < n; q++) {
+        const int c0 = s.ja[k0 + B * q] - 1;
+        if (c0 % B || c0 / B >= I) return;
+        for (int b = 0; b < B; b++)
+          if (s.ja[k + B * q + b] - 1 != c0 + b) return;
+      }
+      for (int t = 0; t < a; t++)
+        if (s.ja[k + B * n + t] - 1 != r0 + t) return;
+    }
+    for (int q = 0; q < n; q++) nup[(s.ja[k0 + B * q] - 1) / B]++;
+  }
+  s.bia.assign(nb + 1, 0);
+  for (int I = 0; I < nb; I++) s.bia[I + 1] = s.bia[I] + nl[I] + 1 + nup[I];
+  const int64_t nnzb = s.bia[nb];
+  s.bja.assign(nnzb, 0);
+  s.bt.assign(nnzb, 0);
+  std::vector<int32_t> upos(nb);
+  for (int I = 0; I < nb; I++) upos[I] = s.bia[I] + nl[I] + 1;
+  for (int I = 0; I < nb; I++) {
+    const int32_t k0 = s.ia[B * I] - 1;
+    const int32_t p0 = s.bia[I];
+    for (int q = 0; q < nl[I]; q++) {
+      const int J = (s.ja[k0 + B * q] - 1) / B;
+      s.bja[p0 + q] = J;
+      s.bt[p0 + q] = -1 - I;
+      // the mirror (I above J) goes to the next upper slot of row J; rows I
+      // arrive in ascending order, so the upper blocks come out sorted
+      const int32_t u = upos[J]++;
+      s.bja[u] = I;
+      s.bt[u] = p0 + q;
+    }
+    s.bja[p0 + nl[I]] = I;
+    s.bt[p0 + nl[I]] = -1 - I;
+  }
+  s.blocked = true;
+  s.bsize = B;
+  s.nb = nb;
+  s.nnzb = nnzb;
+}
+
 }  // namespace elx

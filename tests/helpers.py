@@ -36,6 +36,18 @@ def two_components(m):
                   f=np.vstack([m.f, m.f]), name=m.name + "_x2")
 
 
+def rollers(m, axis=0):
+    """The same mesh with the normal dof of the nodes on the face x_axis = min
+    fixed (rollers): those nodes are only partly fixed, so the equations no
+    longer come in whole node blocks."""
+    m2 = M.Mesh(ndm=m.ndm, ndf=m.ndf, nen=m.nen, x=m.x, ix=m.ix, ie=m.ie, e=m.e,
+                id=m.id.copy(), f=m.f.copy(), name=m.name + "_rollers")
+    face = np.isclose(m.x[:, axis], m.x[:, axis].min())
+    m2.id[face, axis] = 1
+    m2.f[face, axis] = 0.0
+    return m2
+
+
 def row_scaled_error(ia, a_ref, a_got, ad_ref, ad_got):
     """max |delta| over the entries of each row, divided by the row's largest
     |entry| (diagonal included): the assembly parity metric."""

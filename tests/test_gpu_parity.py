@@ -17,7 +17,7 @@ import pytest
 import elastic_gb300 as E
 import oracle as O
 from elastic_gb300 import meshgen as M
-from helpers import relabel_nodes, rel_inf, row_scaled_error, two_components
+from helpers import relabel_nodes, rel_inf, rollers, row_scaled_error, two_components
 
 pytestmark = pytest.mark.gpu
 
@@ -43,6 +43,8 @@ MESHES = {
     "hexa8": lambda: M.box_hexa8(9, 8, 7, jitter=0.2, seed=5),
     "hexa8_scrambled": lambda: relabel_nodes(M.box_hexa8(6, 5, 4), 8),
     "tetra4_two_components": lambda: two_components(M.box_tetra4(3, 3, 3)),
+    # partly fixed nodes: no node blocks, the scalar (two-sided gather) kernels
+    "hexa8_rollers": lambda: rollers(M.box_hexa8(7, 6, 5, jitter=0.1, seed=6)),
 }
 
 
@@ -73,7 +75,7 @@ def test_caller_supplied_structure_matches_built_structure(gpu_ctx):
     assert np.array_equal(ad1, ad2) and np.array_equal(al1, al2)
 
 
-@pytest.mark.parametrize("name", ["quad4_stress", "tetra4", "hexa8"])
+@pytest.mark.parametrize("name", ["quad4_stress", "tetra4", "hexa8", "hexa8_rollers"])
 def test_spmv_parity(gpu_ctx, name):
     m = MESHES[name]()
     s = _setup(gpu_ctx, m)
@@ -84,7 +86,8 @@ def test_spmv_parity(gpu_ctx, name):
     assert rel_inf(y_o, y_g) <= SPMV_TOL
 
 
-@pytest.mark.parametrize("name", ["quad4_stress", "tria3_stress", "tetra4", "hexa8"])
+@pytest.mark.parametrize("name", ["quad4_stress", "tria3_stress", "tetra4", "hexa8",
+                                  "hexa8_rollers"])
 def test_pcg_parity(gpu_ctx, name):
     m = MESHES[name]()
     # every mesh gets a seeded nodal load (some generators carry none)
@@ -101,6 +104,29 @@ def test_pcg_parity(gpu_ctx, name):
     np.testing.assert_allclose(i_g["xkx"], i_o["xkx"], rtol=1e-10)
     np.testing.assert_allclose(i_g["conv"], i_o["conv"], rtol=1e-13)
     assert i_g["norm_m_r"] <= 3.16 * i_g["conv"]
+
+
+@pytest.mark.parametrize("name", ["hexa8", "quad4_stress", "tetra4"])
+def test_block_and_scalar_kernels_agree(gpu_ctx, name, monkeypatch):
+    """The node-block product and the scalar two-sided gather (node blocks
+    switched off) give the oracle's K x, and PCG the same solution."""
+    m = MESHES[name]()
+    s = _setup(gpu_ctx, m)
+    _, ad, al = gpu_ctx.assemble(None, None, want_matrix=True)
+    x = np.random.default_rng(3).standard_normal(s.neq)
+    b = np.random.default_rng(4).standard_normal(s.neq)
+    y_blocks = gpu_ctx.spmv(x)
+    u_blocks, _ = gpu_ctx.solve(b, tol=1e-11, maxit=20000)
+    bytes_blocks = gpu_ctx.device_bytes
+    monkeypatch.setenv("ELX_BLOCKS", "0")
+    _setup(gpu_ctx, m)
+    gpu_ctx.assemble(None, None)
+    y_scalar = gpu_ctx.spmv(x)
+    u_scalar, _ = gpu_ctx.solve(b, tol=1e-11, maxit=20000)
+    assert gpu_ctx.device_bytes != bytes_blocks  # a different matrix layout was resident
+    y_o = O.matvec(s, ad, al, x)
+    assert rel_inf(y_o, y_blocks) <= SPMV_TOL and rel_inf(y_o, y_scalar) <= SPMV_TOL
+    assert rel_inf(u_blocks, u_scalar) <= U_TOL
 
 
 def test_solvm_quad_known_answer(gpu_ctx):

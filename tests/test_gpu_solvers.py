@@ -1,0 +1,142 @@
+"""GPU BiCGSTAB (pbicgstab, Iters.f:1079-1349) and GMRES(k) (gmres,
+Iters.f:528-808) through the C ABI against the oracle's restatements.
+
+Unlike CG, neither method's iteration count is stable under rounding.
+BiCGSTAB's residual is not monotone, and restarted GMRES stagnates for
+long stretches on these elasticity systems; the oracle itself, rerun with
+the same dot products summed in random orders, stops after 110-124
+BiCGSTAB iterations on the 9x8x7 HEXA8 box below (123 in the reference's
+order), after 679-720 GMRES(7) steps there (716), and after 10294-12958
+GMRES(50) steps on the 64x16 QUAD4 cantilever (12400), and those
+solutions differ from the reference-order ones by up to 2.8e-8 relative.
+
+So both solvers are held to:
+  (a) the same iterates as the oracle before rounding has accumulated:
+      after 1 and 6 BiCGSTAB iterations, and after the first GMRES(12)
+      cycle and two GMRES(5) cycles, within 1e-11 relative (inf-norm);
+  (b) at convergence (tol 1e-10): iterations within 15 % of the oracle's,
+      displacements within 1e-7 relative, the same stopping threshold
+      (tol ||b|| for BiCGSTAB, tol ||M b|| for GMRES) within 1e-13, the same
+      xKx within 1e-7, and for BiCGSTAB the reference's exactness check
+      ||b - K x|| <= 3.16 tol ||b|| (Iters.f:1306).
+"""
+import numpy as np
+import pytest
+
+import elastic_gb300 as E
+import oracle as O
+from elastic_gb300 import meshgen as M
+from helpers import rel_inf
+
+pytestmark = pytest.mark.gpu
+
+U_TOL = 1e-7         # converged solutions (see above)
+FIRST_TOL = 1e-11    # early iterates
+
+MESHES = {
+    "quad4_stress": lambda: M.cantilever_quad4_64x16(),
+    "tria3_strain": lambda: M.box2d(12, 9, 2.0, 1.0, etype=M.TRIA3_STRAIN, E=3.0, nu=0.25),
+    "tetra4": lambda: M.box_tetra4(7, 6, 5, jitter=0.2, lognormal_E=True, seed=4),
+    "hexa8": lambda: M.box_hexa8(9, 8, 7, jitter=0.2, seed=5),
+}
+
+
+def _system(ctx, name):
+    m = MESHES[name]()
+    m.f = np.random.default_rng(11).standard_normal(m.f.shape) * (m.id == 0)
+    ctx.set_mesh(m)
+    ctx.build_structure(True)
+    s = O.structure(m, True)
+    b0, u0 = O.loads(m, s)
+    ad, al, b = O.assemble(m, s, u0, b0)
+    ctx.assemble(u0, b0)
+    return s, ad, al, b
+
+
+def _close_at_convergence(i_o, i_g, x_o, x_g):
+    assert i_o["status"] == 0 and i_g["status"] == 0
+    assert abs(i_o["iters"] - i_g["iters"]) <= max(2, 0.15 * i_o["iters"]), \
+        (i_o["iters"], i_g["iters"])
+    assert rel_inf(x_o, x_g) <= U_TOL
+    np.testing.assert_allclose(i_g["conv"], i_o["conv"], rtol=1e-13)
+    np.testing.assert_allclose(i_g["xkx"], i_o["xkx"], rtol=1e-7)
+
+
+@pytest.mark.parametrize("name", sorted(MESHES))
+def test_bicgstab_parity(gpu_ctx, name):
+    s, ad, al, b = _system(gpu_ctx, name)
+    x_o, i_o = O.pbicgstab(s, ad, al, b, tol=1e-10, maxit=20000)
+    x_g, i_g = gpu_ctx.solve(b, solver=E.SOLVER_BICGSTAB, tol=1e-10, maxit=20000)
+    _close_at_convergence(i_o, i_g, x_o, x_g)
+    assert i_g["norm_r"] <= 3.16 * i_g["conv"]
+
+
+@pytest.mark.parametrize("name", sorted(MESHES))
+def test_bicgstab_first_iterates_match(gpu_ctx, name):
+    s, ad, al, b = _system(gpu_ctx, name)
+    for maxit in (1, 6):
+        x_o, i_o = O.pbicgstab(s, ad, al, b, tol=1e-14, maxit=maxit)
+        x_g, i_g = gpu_ctx.solve(b, solver=E.SOLVER_BICGSTAB, tol=1e-14, maxit=maxit,
+                                 raise_on_error=False)
+        assert i_o["status"] == E.ERR_NO_CONVERGENCE and i_g["status"] == E.ERR_NO_CONVERGENCE
+        assert i_g["iters"] == i_o["iters"] == maxit
+        assert rel_inf(x_o, x_g) <= FIRST_TOL, maxit
+
+
+# GMRES(7) stagnates on the 2-D meshes (tens of thousands of steps).
+GMRES_CASES = [(50, n) for n in sorted(MESHES)] + [(7, "hexa8"), (7, "tetra4")]
+
+
+@pytest.mark.parametrize("k,name", GMRES_CASES)
+def test_gmres_parity(gpu_ctx, name, k):
+    s, ad, al, b = _system(gpu_ctx, name)
+    x_o, i_o = O.gmres(s, ad, al, b, k=k, tol=1e-10, maxit=5000)
+    x_g, i_g = gpu_ctx.solve(b, solver=E.SOLVER_GMRES, tol=1e-10, maxit=5000, ngram=k)
+    _close_at_convergence(i_o, i_g, x_o, x_g)
+
+
+@pytest.mark.parametrize("name", sorted(MESHES))
+@pytest.mark.parametrize("k,cycles", [(12, 1), (5, 2)])
+def test_gmres_first_cycles_match(gpu_ctx, name, k, cycles):
+    s, ad, al, b = _system(gpu_ctx, name)
+    x_o, i_o = O.gmres(s, ad, al, b, k=k, tol=1e-14, maxit=cycles)
+    x_g, i_g = gpu_ctx.solve(b, solver=E.SOLVER_GMRES, tol=1e-14, maxit=cycles, ngram=k,
+                             raise_on_error=False)
+    assert i_o["status"] == E.ERR_NO_CONVERGENCE and i_g["status"] == E.ERR_NO_CONVERGENCE
+    assert i_g["iters"] == i_o["iters"] == k * cycles
+    assert rel_inf(x_o, x_g) <= FIRST_TOL
+
+
+@pytest.mark.parametrize("solver", [E.SOLVER_BICGSTAB, E.SOLVER_GMRES])
+def test_solver_runs_are_bitwise_repeatable(gpu_ctx, solver):
+    _, _, _, b = _system(gpu_ctx, "hexa8")
+    x1, i1 = gpu_ctx.solve(b, solver=solver, tol=1e-10, maxit=5000, ngram=20)
+    x2, i2 = gpu_ctx.solve(b, solver=solver, tol=1e-10, maxit=5000, ngram=20)
+    assert np.array_equal(x1, x2) and i1["iters"] == i2["iters"]
+
+
+@pytest.mark.parametrize("solver,maxit", [(E.SOLVER_BICGSTAB, 3), (E.SOLVER_GMRES, 1)])
+def test_solver_reports_no_convergence(gpu_ctx, solver, maxit):
+    """The reference stops the run (stop_mef) when maxit is reached; the
+    library returns ELX_ERR_NO_CONVERGENCE with the iterate reached."""
+    _, _, _, b = _system(gpu_ctx, "hexa8")
+    x, info = gpu_ctx.solve(b, solver=solver, tol=1e-12, maxit=maxit, ngram=5,
+                            raise_on_error=False)
+    assert info["status"] == E.ERR_NO_CONVERGENCE
+    assert np.isfinite(x).all() and np.abs(x).max() > 0
+
+
+def test_gmres_restart_length_is_checked(gpu_ctx):
+    _, _, _, b = _system(gpu_ctx, "quad4_stress")
+    for k in (0, 100000):
+        _, info = gpu_ctx.solve(b, solver=E.SOLVER_GMRES, ngram=k, raise_on_error=False)
+        assert info["status"] == E.ERR_ARG
+
+
+def test_solvers_agree_on_the_solution(gpu_ctx):
+    """PCG, BiCGSTAB and GMRES solve the same SPD system to the same x."""
+    _, _, _, b = _system(gpu_ctx, "tetra4")
+    x_p, _ = gpu_ctx.solve(b, solver=E.SOLVER_PCG, tol=1e-12, maxit=20000)
+    x_b, _ = gpu_ctx.solve(b, solver=E.SOLVER_BICGSTAB, tol=1e-12, maxit=20000)
+    x_g, _ = gpu_ctx.solve(b, solver=E.SOLVER_GMRES, tol=1e-12, maxit=5000, ngram=50)
+    assert rel_inf(x_p, x_b) <= 1e-8 and rel_inf(x_p, x_g) <= 1e-8
