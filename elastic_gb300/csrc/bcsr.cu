@@ -169,6 +169,111 @@ bcsr_spmv_kernel(int neq, const int32_t *__restrict__ bia, const int32_t *__rest
   }
 }
 
+// y = K x with L lanes per block row (FP32): lane l takes blocks l, l + L,
+// .. of the row (a block's B^2 values are contiguous, so consecutive lanes
+// read one contiguous stream), then a fixed shuffle tree adds the lanes' B
+// row sums.  Each group works on R block rows at once, all loads of the R
+// rows issued before their FMAs, so that more bytes are in flight per warp.
+// The FP32 pipe has room for the shuffles; the FP64 product keeps one thread
+// per row (bcsr_spmv_kernel) so that its FP64 pipe does FMAs only.
+template <class T, int B, int L, int R, int EPI>
+__global__ void __launch_bounds__(256)
+bcsr_spmv_group_kernel(int nb, const int32_t *__restrict__ bia, const int32_t *__restrict__ bja,
+                       const T *__restrict__ bval, const T *__restrict__ x, T *__restrict__ y,
+                       const T *__restrict__ w, PcgScalars *sc, double *partials,
+                       unsigned int *counter, const int32_t *gate) {
+  constexpr bool DOT = EPI == kEpiPcg || EPI == kEpiBicgAlpha || EPI == kEpiBicgOmega;
+  constexpr int NV = EPI == kEpiBicgOmega ? 2 : 1;
+  constexpr int BB = B * B;
+  if (DOT && sc->done) return;
+  if (gate && *gate == 0) return;
+  T v[NV];
+#pragma unroll
+  for (int c = 0; c < NV; c++) v[c] = T(0);
+  const int lane = threadIdx.x % L;
+  const int ngroups = gridDim.x * (256 / L);
+  for (int I0 = (blockIdx.x * 256 + threadIdx.x) / L; I0 < nb; I0 += R * ngroups) {
+    int pb[R], pe[R];
+    T acc[R][B];
+    int kmax = 0;
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const int I = I0 + r * ngroups;
+      pb[r] = I < nb ? bia[I] : 0;
+      pe[r] = I < nb ? bia[I + 1] : 0;
+      kmax = max(kmax, pe[r] - pb[r]);
+#pragma unroll
+      for (int a = 0; a < B; a++) acc[r][a] = T(0);
+    }
+    for (int k = lane; k < kmax; k += L) {
+      T xv[R][B], bv[R][BB];
+      bool on[R];
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int p = pb[r] + k;
+        on[r] = p < pe[r];
+        const int J = on[r] ? bja[p] : 0;
+        const T *blk = bval + (size_t)(on[r] ? p : 0) * BB;
+#pragma unroll
+        for (int e = 0; e < BB; e++) bv[r][e] = on[r] ? blk[e] : T(0);
+#pragma unroll
+        for (int b = 0; b < B; b++) xv[r][b] = on[r] ? x[J * B + b] : T(0);
+      }
+#pragma unroll
+      for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int a = 0; a < B; a++)
+#pragma unroll
+          for (int b = 0; b < B; b++) acc[r][a] += bv[r][a * B + b] * xv[r][b];
+    }
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1)
+#pragma unroll
+      for (int r = 0; r < R; r++)
+#pragma unroll
+        for (int a = 0; a < B; a++)
+          acc[r][a] += __shfl_down_sync(0xffffffffu, acc[r][a], off, L);
+    if (lane == 0) {
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int I = I0 + r * ngroups;
+        if (I >= nb) continue;
+#pragma unroll
+        for (int a = 0; a < B; a++) {
+          const int row = I * B + a;
+          T yi = acc[r][a];
+          if (EPI == kEpiScale) yi = yi * w[row];
+          y[row] = yi;
+          if (EPI == kEpiPcg) v[0] += x[row] * yi;
+          if (EPI == kEpiBicgAlpha) v[0] += yi * w[row];
+          if (EPI == kEpiBicgOmega) {
+            v[0] += yi * w[row];
+            v[1] += yi * yi;
+          }
+        }
+      }
+    }
+  }
+  if (!DOT) return;
+  double vb[NV];
+  block_sum_widen<NV>(v, vb);
+  if (!publish_partials<NV>(vb, partials, counter)) return;
+  double tot[NV];
+  gather_partials<NV>(tot, partials, counter);
+  if (threadIdx.x == 0) {
+    if (EPI == kEpiPcg) {
+      sc->pq = tot[0];
+      sc->alpha = sc->d / tot[0];
+    } else if (EPI == kEpiBicgAlpha) {
+      sc->pq = tot[0];
+      sc->alpha = sc->rho / tot[0];
+      sc->iters += 1;
+    } else if (EPI == kEpiBicgOmega) {
+      sc->omega = tot[0] / tot[NV - 1];
+    }
+  }
+}
+
 int fill_grid(int64_t n) {
   const int64_t g = (n + 255) / 256;
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
@@ -212,12 +317,25 @@ void launch_bcsr(const CsrcDev &k, const T *x, T *y, const T *w, PcgScalars *sc,
   // 48^3 TETRA4 mesh
   int grid = std::max(1, std::min((k.neq + 255) / 256, 1216));
   if (k.gather_blocks > 0) grid = std::min((k.neq + 255) / 256, k.gather_blocks);
-  if (k.bsize == 3)
+  if (sizeof(T) == 4 && k.group_lanes > 0) {
+    // lane groups per block row (FP32); two rows in flight per group measured
+    // slower (register pressure): 78.6 against 68.8 us on the 64^3 HEXA8 cube
+    if (k.bsize == 3 && k.group_lanes == 8)
+      bcsr_spmv_group_kernel<T, 3, 8, 1, EPI><<<grid, 256, 0, st>>>(
+          k.nb, k.bia, k.bja, val, x, y, w, sc, partials, counter, gate);
+    else if (k.bsize == 3)
+      bcsr_spmv_group_kernel<T, 3, 16, 1, EPI><<<grid, 256, 0, st>>>(
+          k.nb, k.bia, k.bja, val, x, y, w, sc, partials, counter, gate);
+    else
+      bcsr_spmv_group_kernel<T, 2, 8, 1, EPI><<<grid, 256, 0, st>>>(
+          k.nb, k.bia, k.bja, val, x, y, w, sc, partials, counter, gate);
+  } else if (k.bsize == 3) {
     bcsr_spmv_kernel<T, 3, EPI, 3><<<grid, 256, 0, st>>>(k.neq, k.bia, k.bja, val, x, y, w, sc,
                                                          partials, counter, gate);
-  else
+  } else {
     bcsr_spmv_kernel<T, 2, EPI, 4><<<grid, 256, 0, st>>>(k.neq, k.bia, k.bja, val, x, y, w, sc,
                                                          partials, counter, gate);
+  }
   ELX_CUDA(cudaGetLastError());
 }
 

@@ -160,6 +160,7 @@ struct CsrcDev {
   const int32_t *bia = nullptr, *bja = nullptr, *bt = nullptr;
   double *bval = nullptr;
   float *bval32 = nullptr;
+  int32_t group_lanes = 16;  // FP32 node-block product: lanes per block row (16 or 32)
 };
 
 struct TileDev {
