@@ -115,6 +115,11 @@ def load():
         "elx_get_rhs": (C.c_int, [_VP, _F64]),
         "elx_spmv_dot_noalloc": (C.c_int, [C.c_int32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                            _VP, _VP, _VP]),
+        "elx_solve_block": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                      C.c_int32, _VP, _VP, _VP]),
+        "elx_solve_block_device": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_double, C.c_int32,
+                                             C.c_int32, _VP, _VP, _VP]),
+        "elx_autotune_block": (C.c_int, [_VP, C.c_int32, P(C.c_int32), _VP]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -297,6 +302,37 @@ class Context:
         d = info.as_dict()
         d["status"] = st if st != OK else d["status"]
         return x, d
+
+    def solve_block(self, B, precision=PREC_MIXED, tol=1e-8, maxit=20000, width=0,
+                    raise_on_error=True):
+        """Block PCG for the columns of B (neq x nrhs): returns (X, infos)."""
+        B = np.asfortranarray(B, dtype=np.float64)
+        if B.ndim == 1:
+            B = B[:, None]
+        neq, nrhs = B.shape
+        X = np.zeros((neq, nrhs), order="F")
+        infos = (Info * nrhs)()
+        st = self._L.elx_solve_block(self._h, nrhs, precision, tol, maxit, width,
+                                     B.ctypes.data_as(_VP), X.ctypes.data_as(_VP), infos)
+        if raise_on_error:
+            self._check(st)
+        return X, [i.as_dict() for i in infos]
+
+    def solve_block_device(self, b_ptr, x_ptr, nrhs, precision=PREC_MIXED, tol=1e-8,
+                           maxit=20000, width=0):
+        """Block PCG on device arrays (pointers to neq x nrhs column-major)."""
+        infos = (Info * nrhs)()
+        self._check(self._L.elx_solve_block_device(self._h, nrhs, precision, tol, maxit, width,
+                                                   _VP(b_ptr), _VP(x_ptr), infos))
+        return [i.as_dict() for i in infos]
+
+    def autotune_block(self, precision=PREC_MIXED, remeasure=False):
+        """(width, product times in us for widths 1, 2, 4, 8, 16 or None)."""
+        w = C.c_int32(0)
+        t = np.zeros(5)
+        self._check(self._L.elx_autotune_block(self._h, precision, C.byref(w),
+                                               t.ctypes.data_as(_VP) if remeasure else None))
+        return w.value, (t if remeasure else None)
 
     def spmv(self, x, precision=PREC_FP64):
         neq, _, _ = self.sizes()

@@ -48,6 +48,14 @@ struct elx_ctx {
   DBuf m32, p32, q32, r32, x32;
   // BiCGSTAB (r0, t) and GMRES (Krylov basis, small dense arrays, state)
   DBuf r0v, tv, gbasis, garrays, gstate;
+  // block PCG: multi-vectors of up to blk_cap columns, scalars, staging
+  DBuf bk_b, bk_x, bk_r, bk_p, bk_q, bk_z, bk_xlo, bk_r32, bk_p32, bk_q32, bk_cols, bk_hdr,
+      bk_part, bk_cnt, bk_diag, bk_colmajor;
+  int blk_cap = 0;
+  int tuned_width[2] = {0, 0};  // autotuned block width (FP64, mixed)
+  cudaGraphExec_t block_graph = nullptr;
+  int block_graph_w = 0;
+  bool block_graph_mixed = false;
   // scalars, partials, counters, flags
   DBuf scal, partials, counters, flags, diag;
   elx::PcgScalars *h_scal = nullptr;  // pinned, 2 slots
@@ -63,6 +71,7 @@ struct elx_ctx {
   int gmres_k = 0, gmres_launches = 0;
   int pcg_graph_iters = 0;
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaEvent_t ev_t[2] = {nullptr, nullptr};  // timing (autotuner)
 
   void alloc(DBuf &d, size_t bytes) {
     release(d);
@@ -100,7 +109,9 @@ struct elx_ctx {
     if (pcg32_graph) cudaGraphExecDestroy(pcg32_graph);
     if (bicg_graph) cudaGraphExecDestroy(bicg_graph);
     if (gmres_graph) cudaGraphExecDestroy(gmres_graph);
-    pcg_graph = pcg32_graph = bicg_graph = gmres_graph = nullptr;
+    if (block_graph) cudaGraphExecDestroy(block_graph);
+    pcg_graph = pcg32_graph = bicg_graph = gmres_graph = block_graph = nullptr;
+    block_graph_w = 0;
     gmres_k = gmres_launches = 0;
     pcg_graph_iters = 0;
   }
@@ -166,6 +177,14 @@ int guarded(elx_ctx *ctx, F &&f) {
 
 void require(bool c, int code, const char *what) {
   if (!c) throw Error{code, what};
+}
+
+void release_block(elx_ctx *c) {
+  for (DBuf *v : {&c->bk_b, &c->bk_x, &c->bk_r, &c->bk_p, &c->bk_q, &c->bk_z, &c->bk_xlo,
+                  &c->bk_r32, &c->bk_p32, &c->bk_q32, &c->bk_cols, &c->bk_hdr, &c->bk_part,
+                  &c->bk_cnt, &c->bk_diag, &c->bk_colmajor})
+    c->release(*v);
+  c->blk_cap = 0;
 }
 
 // Rows per SpMV tile: the largest candidate whose three-stage FP64 pipeline
@@ -276,6 +295,8 @@ void upload_structure(elx_ctx *c) {
   for (DBuf *v : {&c->ad32, &c->al32, &c->alt32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32,
                   &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate})
     c->release(*v);
+  release_block(c);
+  c->tuned_width[0] = c->tuned_width[1] = 0;
   c->have_fp32 = false;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
@@ -695,6 +716,214 @@ void gmres64(elx_ctx *c, int kdim, double tol, int maxit, elx_info *info) {
                                  " cycles (" + std::to_string(st.nit) + " iterations)"};
 }
 
+// ---------------------------------------------------------------- block PCG
+
+constexpr int kMaxBlockWidth = 16;
+
+// Device arrays for blocks of up to `cap` columns (FP32 ones only for the
+// mixed solver), allocated on first use.
+void ensure_block(elx_ctx *c, int cap, bool mixed) {
+  const size_t n = (size_t)c->s.neq;
+  if (c->blk_cap < cap) {
+    release_block(c);
+    if (c->block_graph) cudaGraphExecDestroy(c->block_graph);
+    c->block_graph = nullptr;
+    c->block_graph_w = 0;
+    for (DBuf *v : {&c->bk_b, &c->bk_x, &c->bk_r, &c->bk_p, &c->bk_q, &c->bk_z, &c->bk_colmajor})
+      c->alloc(*v, n * cap * 8);
+    c->alloc(c->bk_cols, sizeof(elx::ColScalars) * kMaxBlockWidth);
+    c->alloc(c->bk_hdr, sizeof(elx::BlockHeader) * 2);
+    c->alloc(c->bk_part, sizeof(double) * 2 * kMaxBlockWidth * 1216);
+    c->alloc(c->bk_cnt, sizeof(unsigned int) * 8);
+    ELX_CUDA(cudaMemsetAsync(c->bk_cnt.p, 0, c->bk_cnt.bytes, c->stream));
+    c->alloc(c->bk_diag, sizeof(double) * 4 * kMaxBlockWidth);
+    elx::BlockHeader on{};
+    on.active = 1;
+    ELX_CUDA(cudaMemcpyAsync(c->bk_hdr.as<elx::BlockHeader>() + 1, &on, sizeof(on),
+                             cudaMemcpyHostToDevice, c->stream));
+    c->sync();
+    c->blk_cap = cap;
+  }
+  if (mixed && !c->bk_xlo.p) {
+    for (DBuf *v : {&c->bk_xlo, &c->bk_r32, &c->bk_p32, &c->bk_q32})
+      c->alloc(*v, n * c->blk_cap * 4);
+    if (c->block_graph) cudaGraphExecDestroy(c->block_graph);
+    c->block_graph = nullptr;
+    c->block_graph_w = 0;
+  }
+}
+
+elx::BlockVecs block_vecs(elx_ctx *c, int w) {
+  elx::BlockVecs v;
+  v.w = w;
+  v.b = c->bk_b.as<double>(); v.m = c->m.as<double>();
+  v.x = c->bk_x.as<double>(); v.r = c->bk_r.as<double>(); v.p = c->bk_p.as<double>();
+  v.q = c->bk_q.as<double>(); v.z = c->bk_z.as<double>();
+  v.m32 = c->m32.as<float>();
+  v.xlo = c->bk_xlo.as<float>(); v.r32 = c->bk_r32.as<float>(); v.p32 = c->bk_p32.as<float>();
+  v.q32 = c->bk_q32.as<float>();
+  v.cols = c->bk_cols.as<elx::ColScalars>();
+  v.hdr = c->bk_hdr.as<elx::BlockHeader>();
+  v.hdr_on = v.hdr + 1;
+  v.partials = c->bk_part.as<double>();
+  v.counters = c->bk_cnt.as<unsigned int>();
+  return v;
+}
+
+// The block width whose product costs least per column: each supported
+// width's SpMM timed on the resident matrix (FP32 for the mixed solver, FP64
+// otherwise), best of three launches after one warm-up.
+int autotune_block_width(elx_ctx *c, bool mixed, double *times_us = nullptr) {
+  const int slot = mixed ? 1 : 0;
+  if (c->tuned_width[slot] && !times_us) return c->tuned_width[slot];
+  ensure_block(c, kMaxBlockWidth, mixed);
+  if (mixed) ensure_fp32(c);
+  const size_t n = (size_t)c->s.neq;
+  ELX_CUDA(cudaMemsetAsync(c->bk_p.p, 0, n * kMaxBlockWidth * 8, c->stream));
+  if (mixed) ELX_CUDA(cudaMemsetAsync(c->bk_p32.p, 0, n * kMaxBlockWidth * 4, c->stream));
+  const elx::CsrcDev k = c->csrc_dev();
+  int best = 1;
+  double best_cost = 1e300;
+  int idx = 0;
+  for (int w : {1, 2, 4, 8, 16}) {
+    const elx::BlockVecs v = block_vecs(c, w);
+    double t_best = 1e300;
+    for (int rep = 0; rep < 4; rep++) {
+      ELX_CUDA(cudaEventRecord(c->ev_t[0], c->stream));
+      if (mixed)
+        elx::launch_spmm32(k, v, c->stream);
+      else
+        elx::launch_spmm64(k, v, c->stream);
+      ELX_CUDA(cudaEventRecord(c->ev_t[1], c->stream));
+      ELX_CUDA(cudaEventSynchronize(c->ev_t[1]));
+      float ms = 0.f;
+      ELX_CUDA(cudaEventElapsedTime(&ms, c->ev_t[0], c->ev_t[1]));
+      if (rep > 0) t_best = std::min(t_best, (double)ms);
+    }
+    c->launches += 4;
+    if (times_us) times_us[idx] = t_best * 1e3;
+    idx++;
+    const double cost = t_best / w;
+    if (cost < best_cost * 0.97) {  // a wider block must win by 3 %
+      best_cost = cost;
+      best = w;
+    }
+  }
+  c->tuned_width[slot] = best;
+  return best;
+}
+
+// Solves nrhs load cases (b column-major, neq x nrhs, on the host or the
+// device) in blocks of `width` columns; x likewise; one elx_info per column.
+void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int width,
+                 const double *b, double *x, elx_info *infos, bool device_ptrs) {
+  require(c->have_matrix, ELX_ERR_STATE, "solve before the matrix is assembled");
+  require(nrhs >= 1 && tol > 0 && maxit >= 0, ELX_ERR_ARG, "bad block solve arguments");
+  require(precision == ELX_PREC_FP64 || precision == ELX_PREC_MIXED, ELX_ERR_ARG,
+          "unknown precision");
+  require(width == 0 || elx::block_width_supported(width), ELX_ERR_ARG,
+          "block width must be 0 (autotune), 1, 2, 4, 8 or 16");
+  require(c->use_blocks, ELX_ERR_ARG,
+          "block solves need node blocks (every node all free or all fixed)");
+  const bool mixed = precision == ELX_PREC_MIXED;
+  auto t0 = std::chrono::steady_clock::now();
+  if (mixed) ensure_fp32(c);
+  build_preconditioner(c);
+  if (width == 0) width = autotune_block_width(c, mixed);
+  int w = 1;
+  while (w < width && w < nrhs) w *= 2;
+  ensure_block(c, std::max(w, c->blk_cap), mixed);
+  const size_t n = (size_t)c->s.neq;
+  const elx::CsrcDev k = c->csrc_dev();
+  const elx::BlockVecs v = block_vecs(c, w);
+  if (!c->block_graph || c->block_graph_w != w || c->block_graph_mixed != mixed) {
+    if (c->block_graph) cudaGraphExecDestroy(c->block_graph);
+    c->block_graph = nullptr;
+    cudaGraph_t g;
+    ELX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (int i = 0; i < kBatch; i++)
+        elx::launch_block_iteration(k, v, mixed, i % kReplaceEvery == kReplaceEvery - 1,
+                                    c->stream);
+    } catch (...) {
+      cudaStreamEndCapture(c->stream, &g);
+      throw;
+    }
+    ELX_CUDA(cudaStreamEndCapture(c->stream, &g));
+    const cudaError_t inst = cudaGraphInstantiate(&c->block_graph, g, 0);
+    cudaGraphDestroy(g);
+    ELX_CUDA(inst);
+    c->block_graph_w = w;
+    c->block_graph_mixed = mixed;
+  }
+  const double per_iter = mixed ? 3 + 3.0 / kReplaceEvery : 3;
+  int status = ELX_OK;
+  for (int c0 = 0; c0 < nrhs; c0 += w) {
+    const int nc = std::min(w, nrhs - c0);
+    // b columns -> column-major staging (zero columns pad a short block)
+    if (nc < w)
+      ELX_CUDA(cudaMemsetAsync(c->bk_colmajor.p, 0, n * w * 8, c->stream));
+    ELX_CUDA(cudaMemcpyAsync(c->bk_colmajor.p, b + (size_t)c0 * n, n * nc * 8,
+                             device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             c->stream));
+    elx::launch_interleave((int)n, w, c->bk_colmajor.as<double>(), c->bk_b.as<double>(),
+                           c->stream);
+    elx::BlockHeader h{};
+    h.tol = tol;
+    h.delta = 0.1;
+    h.maxit = maxit;
+    ELX_CUDA(cudaMemcpyAsync(v.hdr, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
+    elx::launch_block_start(k, v, mixed, c->stream);
+    c->launches += 2;
+    // batches of kBatch iterations until no column is active
+    elx::BlockHeader hh{};
+    const int max_batches = maxit / kBatch + 2;
+    for (int bt = 0; bt < max_batches; bt++) {
+      ELX_CUDA(cudaGraphLaunch(c->block_graph, c->stream));
+      c->launches += (int64_t)(per_iter * kBatch + 0.5);
+      ELX_CUDA(cudaMemcpyAsync(&hh, v.hdr, sizeof(hh), cudaMemcpyDeviceToHost, c->stream));
+      c->sync();
+      if (hh.active == 0) break;
+    }
+    elx::launch_block_diagnostics(k, v, c->bk_diag.as<double>(), c->stream);
+    c->launches += 3;
+    elx::launch_deinterleave((int)n, w, c->bk_x.as<double>(), c->bk_colmajor.as<double>(),
+                             c->stream);
+    c->launches += 1;
+    ELX_CUDA(cudaMemcpyAsync(x + (size_t)c0 * n, c->bk_colmajor.p, n * nc * 8,
+                             device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             c->stream));
+    elx::ColScalars cs[kMaxBlockWidth];
+    double dg[4 * kMaxBlockWidth];
+    ELX_CUDA(cudaMemcpyAsync(cs, v.cols, sizeof(elx::ColScalars) * w, cudaMemcpyDeviceToHost,
+                             c->stream));
+    ELX_CUDA(cudaMemcpyAsync(dg, c->bk_diag.p, sizeof(double) * 4 * w, cudaMemcpyDeviceToHost,
+                             c->stream));
+    c->sync();
+    const double secs =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (int j = 0; j < nc; j++) {
+      const elx::ColScalars &s = cs[j];
+      int st = s.done ? s.status : ELX_ERR_NO_CONVERGENCE;
+      if (st != ELX_OK && status == ELX_OK) status = st;
+      if (!infos) continue;
+      elx_info &in = infos[c0 + j];
+      std::memset(&in, 0, sizeof(in));
+      in.iters = s.iters;
+      in.status = st;
+      in.xkx = dg[4 * j + 0];
+      in.norm_x = std::sqrt(dg[4 * j + 1]);
+      in.norm_m_r = std::sqrt(std::fabs(dg[4 * j + 2]));
+      in.norm_r = std::sqrt(dg[4 * j + 3]);
+      in.conv = s.conv;
+      in.seconds = secs;
+      in.refinements = mixed ? s.nupdates : 0;
+      in.inner_iters = mixed ? s.iters : 0;
+    }
+  }
+  if (status != ELX_OK) throw Error{status, "block PCG: a load case did not converge"};
+}
+
 void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit, int ngram,
                     elx_info *info) {
   require(c->have_matrix, ELX_ERR_STATE, "solve before the matrix is assembled");
@@ -800,6 +1029,7 @@ int elx_create(elx_ctx **out, const elx_opts *opts) {
     ELX_CUDA(cudaHostAlloc(&c->h_diag, 8 * sizeof(double), cudaHostAllocDefault));
     ELX_CUDA(cudaHostAlloc(&c->h_flags, 4 * sizeof(int32_t), cudaHostAllocDefault));
     for (auto &e : c->ev) ELX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &e : c->ev_t) ELX_CUDA(cudaEventCreate(&e));
   });
   if (st != ELX_OK) {
     // keep the context so that elx_last_error can report why
@@ -827,6 +1057,9 @@ void elx_destroy(elx_ctx *c) {
     c->release(*d);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
+  for (auto &e : c->ev_t)
+    if (e) cudaEventDestroy(e);
+  release_block(c);
   if (c->h_scal) cudaFreeHost(c->h_scal);
   if (c->h_diag) cudaFreeHost(c->h_diag);
   if (c->h_flags) cudaFreeHost(c->h_flags);
@@ -1043,6 +1276,34 @@ int elx_solve(elx_ctx *c, int32_t solver, int32_t precision, double tol, int32_t
                              c->stream));
     c->sync();
     if (st != ELX_OK) throw Error{st, c->err};
+  });
+}
+
+int elx_solve_block(elx_ctx *c, int32_t nrhs, int32_t precision, double tol, int32_t maxit,
+                    int32_t width, const double *b, double *x, elx_info *info) {
+  return guarded(c, [&] {
+    require(b && x, ELX_ERR_ARG, "null b or x");
+    solve_block(c, nrhs, precision, tol, maxit, width, b, x, info, false);
+  });
+}
+
+int elx_solve_block_device(elx_ctx *c, int32_t nrhs, int32_t precision, double tol,
+                           int32_t maxit, int32_t width, const double *b, double *x,
+                           elx_info *info) {
+  return guarded(c, [&] {
+    require(b && x, ELX_ERR_ARG, "null b or x");
+    solve_block(c, nrhs, precision, tol, maxit, width, b, x, info, true);
+  });
+}
+
+int elx_autotune_block(elx_ctx *c, int32_t precision, int32_t *width, double *times_us) {
+  return guarded(c, [&] {
+    require(c->have_matrix, ELX_ERR_STATE, "autotune before the matrix is assembled");
+    require(c->use_blocks, ELX_ERR_ARG, "block solves need node blocks");
+    require(width, ELX_ERR_ARG, "null width");
+    const bool mixed = precision == ELX_PREC_MIXED;
+    if (times_us) c->tuned_width[mixed ? 1 : 0] = 0;
+    *width = autotune_block_width(c, mixed, times_us);
   });
 }
 

@@ -40,6 +40,44 @@ struct GmresState {
   int32_t status;
 };
 
+// Block PCG (block_pcg.cu): per-column scalars, a header shared by the
+// columns, and the device arrays of one block of W columns (multi-vectors
+// row-interleaved: entry (row, c) at row * W + c).
+struct ColScalars {
+  double d, alpha, beta, pq, rmax, conv, bmb;
+  int32_t iters, done, status, update, nupdates, pad;
+};
+struct BlockHeader {
+  double tol;      // (input)
+  double delta;    // mixed precision: replacement threshold (input)
+  int32_t maxit;   // (input)
+  int32_t active;  // columns still iterating
+  int32_t any_update;
+  int32_t pad;
+};
+struct BlockVecs {
+  int w = 0;
+  const double *b = nullptr, *m = nullptr;
+  double *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *z = nullptr;
+  const float *m32 = nullptr;
+  float *xlo = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr;
+  ColScalars *cols = nullptr;
+  BlockHeader *hdr = nullptr;     // the solve's header
+  BlockHeader *hdr_on = nullptr;  // a header with active = 1 (products outside a solve)
+  double *partials = nullptr;     // 2 * 16 * 1216 doubles
+  unsigned int *counters = nullptr;  // 8
+};
+bool block_width_supported(int w);
+void launch_block_start(const CsrcDev &k, const BlockVecs &v, bool mixed, cudaStream_t st);
+void launch_block_iteration(const CsrcDev &k, const BlockVecs &v, bool mixed,
+                            bool replacement_point, cudaStream_t st);
+void launch_block_diagnostics(const CsrcDev &k, const BlockVecs &v, double *out,
+                              cudaStream_t st);
+void launch_spmm32(const CsrcDev &k, const BlockVecs &v, cudaStream_t st);  // q32 = K p32
+void launch_spmm64(const CsrcDev &k, const BlockVecs &v, cudaStream_t st);  // q = K p
+void launch_interleave(int n, int w, const double *colmajor, double *inter, cudaStream_t st);
+void launch_deinterleave(int n, int w, const double *inter, double *colmajor, cudaStream_t st);
+
 int vector_grid(int n);
 
 // SpMV kernel families (spmv.cu)

@@ -88,8 +88,11 @@ __device__ __forceinline__ void gather_partials(double (&tot)[NV], const double 
 #pragma unroll
   for (int i = 0; i < NV; i++) {
     double s = 0.0;
+    // L2 loads (__ldcg: the partials were written by other blocks, ordered by
+    // the fence + ticket); several in flight per thread
+#pragma unroll 4
     for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads)
-      s += ((volatile const double *)partials)[(size_t)i * gridDim.x + b];
+      s += __ldcg(partials + (size_t)i * gridDim.x + b);
     tot[i] = s;
   }
   block_sum<NV>(tot);

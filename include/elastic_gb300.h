@@ -157,6 +157,27 @@ int elx_solve(elx_ctx *ctx, int32_t solver, int32_t precision, double tol,
               int32_t maxit, int32_t ngram, const double *b, double *x,
               elx_info *info);
 
+/* Block PCG: nrhs load cases of the resident matrix, solved `width`
+ * columns at a time over one read of the matrix per iteration (each column is
+ * the reference's Jacobi PCG with its own scalars and stopping test; pcg,
+ * Iters.f:252-524).  b and x are neq x nrhs, column-major; info has nrhs
+ * entries (refinements = FP64 residual replacements of the mixed solver).
+ * width 0 = autotuned (elx_autotune_block); otherwise 1, 2, 4, 8 or 16.
+ * Needs node blocks: every node all free or all fixed.  No reference
+ * counterpart (the reference solves one load case per solv call,
+ * Main.f:820-826).  _device: b and x are device pointers. */
+int elx_solve_block(elx_ctx *ctx, int32_t nrhs, int32_t precision, double tol,
+                    int32_t maxit, int32_t width, const double *b, double *x,
+                    elx_info *info);
+int elx_solve_block_device(elx_ctx *ctx, int32_t nrhs, int32_t precision, double tol,
+                           int32_t maxit, int32_t width, const double *b, double *x,
+                           elx_info *info);
+/* The block width with the least product time per column on the resident
+ * matrix (FP32 product for ELX_PREC_MIXED, FP64 otherwise); times_us
+ * (nullable, 5 entries) gets the product times of widths 1, 2, 4, 8, 16 and
+ * forces a new measurement. */
+int elx_autotune_block(elx_ctx *ctx, int32_t precision, int32_t *width, double *times_us);
+
 /* update_mec (Predict.f:183-209): u(j,i) = x(id(j,i)) for free dofs. */
 int elx_update(elx_ctx *ctx, const double *x, double *u);
 
