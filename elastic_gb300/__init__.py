@@ -20,7 +20,8 @@ from dataclasses import dataclass
 
 import numpy as np
 
-__all__ = ["ElasticError", "Context", "Info", "load", "library_path", "pform_mec", "solv",
+__all__ = ["ElasticError", "Context", "Server", "Info", "load", "library_path", "pform_mec",
+           "solv",
            "host_structure",
            "solvm", "SOLVER_PCG", "SOLVER_GMRES", "SOLVER_BICGSTAB", "PREC_FP64",
            "PREC_MIXED"]
@@ -56,6 +57,20 @@ class Info(C.Structure):
                 ("norm_x", C.c_double), ("norm_r", C.c_double), ("norm_m_r", C.c_double),
                 ("conv", C.c_double), ("seconds", C.c_double), ("mflops", C.c_double),
                 ("refinements", C.c_int32), ("inner_iters", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("prep_threads", C.c_int32), ("hbm_budget", C.c_int64),
+                ("poll_steps", C.c_int32), ("max_slots", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("peak_bytes", C.c_int64),
+                ("resident_bytes", C.c_int64), ("peak_slots", C.c_int64),
+                ("iterations", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -120,6 +135,14 @@ def load():
         "elx_solve_block_device": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                              C.c_int32, _VP, _VP, _VP]),
         "elx_autotune_block": (C.c_int, [_VP, C.c_int32, P(C.c_int32), _VP]),
+        "elx_server_create": (C.c_int, [P(_VP), P(ServerOpts)]),
+        "elx_server_destroy": (None, [_VP]),
+        "elx_server_submit": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                        C.c_int32, _I32, _F64, _I32, _F64, C.c_int32,
+                                        C.c_int32, _I32, C.c_int32, _F64, C.c_double,
+                                        C.c_int32, P(C.c_int64)]),
+        "elx_server_wait": (C.c_int, [_VP, C.c_int64, C.c_double, _VP, _VP, P(C.c_double)]),
+        "elx_server_get_stats": (C.c_int, [_VP, P(ServerStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -467,3 +490,69 @@ def solvm(mesh, tol=1e-11, maxit=10000, maxnlit=2, nl_tol=1e-4, solver=SOLVER_PC
     if own:
         return u, info, ctx
     return u, info, ctx
+
+
+class Server:
+    """Solve server (elx_server_*): submit meshes with load cases, collect
+    nodal displacements; requests are batched continuously on the GPU."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0, prep_threads: int = 4,
+                 poll_steps: int = 8, max_slots: int = 4096):
+        self._L = load()
+        self._h = _VP()
+        o = ServerOpts(device, prep_threads, hbm_budget, poll_steps, max_slots)
+        st = self._L.elx_server_create(C.byref(self._h), C.byref(o))
+        if st != OK:
+            raise ElasticError(st, "server creation failed")
+        self._shapes = {}
+
+    def submit(self, mesh, F, tol=1e-8, maxit=20000) -> int:
+        """F: nodal forces (nnode, ndf) or (nrhs, nnode, ndf).  Returns a ticket."""
+        F = np.ascontiguousarray(F, dtype=np.float64)
+        if F.ndim == 2:
+            F = F[None]
+        e = _f64(mesh.e)
+        t = C.c_int64(0)
+        st = self._L.elx_server_submit(self._h, mesh.ndm, mesh.ndf, mesh.nen, mesh.numel,
+                                       mesh.nnode, _i32(mesh.ix), _f64(mesh.x), _i32(mesh.ie),
+                                       e, e.shape[1], e.shape[0], _i32(mesh.id), F.shape[0],
+                                       F, tol, maxit, C.byref(t))
+        if st != OK:
+            raise ElasticError(st, "submit failed")
+        self._shapes[t.value] = F.shape
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0):
+        """(U (nrhs, nnode, ndf), infos, latency_s, status); raises on timeout."""
+        shape = self._shapes[ticket]
+        U = np.zeros(shape)
+        infos = (Info * shape[0])()
+        lat = C.c_double(0)
+        st = self._L.elx_server_wait(self._h, ticket, timeout, U.ctypes.data_as(_VP),
+                                     C.cast(infos, _VP), C.byref(lat))
+        if st == ERR_TIMEOUT:
+            raise ElasticError(st, "request not done yet")
+        del self._shapes[ticket]
+        return U, [i.as_dict() for i in infos], lat.value, st
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        self._L.elx_server_get_stats(self._h, C.byref(s))
+        return s.as_dict()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.elx_server_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -337,3 +337,34 @@ def element_dets(mesh: Mesh) -> np.ndarray:
     b = xs[:, 1] - xs[:, 3]
     c = xs[:, 2] - xs[:, 3]
     return np.einsum("ij,ij->i", a, np.cross(b, c))
+
+
+def serving_request(rng, dof_min=2e3, dof_max=2e6, max_rhs=8):
+    """One request of the served stream: a structured box mesh with element
+    type uniform over {TRIA3, QUAD4, TETRA4, HEXA8} (plane stress in 2-D),
+    about log-uniform [dof_min, dof_max] dofs, E ~ U[0.5, 2], nu ~ U[0.2, 0.45],
+    one face fixed (whole nodes) and 1..max_rhs load cases of N(0,1) nodal
+    forces on the opposite face.  Returns (mesh, F) with F (nrhs, nnode, ndf)."""
+    etype = int(rng.choice([TRIA3_STRESS, QUAD4_STRESS, TETRA4, HEXA8]))
+    dof = float(np.exp(rng.uniform(np.log(dof_min), np.log(dof_max))))
+    E = float(rng.uniform(0.5, 2.0))
+    nu = float(rng.uniform(0.2, 0.45))
+    nrhs = int(rng.integers(1, max_rhs + 1))
+    if NDM_OF_TYPE[etype] == 2:
+        # (nx+1)(ny+1) nodes, 2 dofs each, nx = 2 ny
+        ny = max(2, int(round(np.sqrt(dof / 4.0))))
+        nx = 2 * ny
+        m = box2d(nx, ny, 2.0, 1.0, etype=etype, E=E, nu=nu, clamp="left")
+        far = np.isclose(m.x[:, 0], 2.0)
+    else:
+        n = max(2, int(round((dof / 3.0) ** (1.0 / 3.0))) - 1)
+        if etype == HEXA8:
+            m = box_hexa8(n, n, n, E=E, nu=nu, pressure=0.0)
+        else:
+            m = box_tetra4(n, n, n, E=E, nu=nu, pressure=0.0)
+        far = np.isclose(m.x[:, 2], 1.0)
+    F = np.zeros((nrhs, m.nnode, m.ndf))
+    for k in range(nrhs):
+        F[k][far] = rng.standard_normal((int(far.sum()), m.ndf))
+    m.f = F[0].copy()
+    return m, F

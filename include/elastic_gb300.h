@@ -178,6 +178,50 @@ int elx_solve_block_device(elx_ctx *ctx, int32_t nrhs, int32_t precision, double
  * forces a new measurement. */
 int elx_autotune_block(elx_ctx *ctx, int32_t precision, int32_t *width, double *times_us);
 
+/* ---- solve server ----------------------------------------------------- */
+/* A request loop over many meshes at once (no reference counterpart: the
+ * reference runs one deck per process).  Requests are solved with the
+ * reference's FP64 Jacobi PCG; structures are built on host threads while
+ * the GPU works; a request is admitted when its device memory fits the HBM
+ * budget; the PCG iterations of all admitted requests (every load case) run
+ * as one packed set of kernels per iteration, each load case with its own
+ * scalars and stopping test; requests join and leave between polls
+ * (continuous batching).  A result is bitwise the same alone and in a mix. */
+typedef struct elx_server elx_server;
+typedef struct elx_server_opts {
+  int32_t device;
+  int32_t prep_threads; /* host threads building structures (0: 4)          */
+  int64_t hbm_budget;   /* device bytes for admitted requests (0: no limit)  */
+  int32_t poll_steps;   /* PCG iterations between polls (0: 8)               */
+  int32_t max_slots;    /* load cases in flight at most (0: 4096)            */
+} elx_server_opts;
+typedef struct elx_server_stats {
+  int64_t submitted, completed;
+  int64_t peak_bytes;     /* most device bytes held by admitted requests      */
+  int64_t resident_bytes; /* bytes held now                                   */
+  int64_t peak_slots;     /* most load cases in one packed iteration         */
+  int64_t iterations;     /* packed iterations run                           */
+} elx_server_stats;
+int elx_server_create(elx_server **out, const elx_server_opts *opts);
+/* Queues a request (the arrays are copied): a mesh as for elx_set_mesh,
+ * bc(ndf,nnode) with 1 = constrained (whole nodes: a node's dofs all free or
+ * all fixed), f(ndf,nnode,nrhs) nodal forces per load case.  Returns at
+ * once with a ticket. */
+int elx_server_submit(elx_server *srv, int32_t ndm, int32_t ndf, int32_t nen,
+                      int32_t numel, int32_t nnode, const int32_t *ix, const double *x,
+                      const int32_t *ie, const double *e, int32_t prop, int32_t numat,
+                      const int32_t *bc, int32_t nrhs, const double *f, double tol,
+                      int32_t maxit, int64_t *ticket);
+/* Waits (timeout_s < 0: without limit) for a request; u(ndf,nnode,nrhs)
+ * gets the displacements (0 on fixed dofs), info[nrhs] the per-load-case
+ * iterations, status and threshold, latency_s submit-to-done seconds.
+ * Returns the request's status (ELX_ERR_TIMEOUT: not done yet; the ticket
+ * stays valid).  Each ticket can be collected once. */
+int elx_server_wait(elx_server *srv, int64_t ticket, double timeout_s, double *u,
+                    elx_info *info, double *latency_s);
+int elx_server_get_stats(elx_server *srv, elx_server_stats *stats);
+void elx_server_destroy(elx_server *srv);
+
 /* update_mec (Predict.f:183-209): u(j,i) = x(id(j,i)) for free dofs. */
 int elx_update(elx_ctx *ctx, const double *x, double *u);
 
