@@ -229,16 +229,18 @@ def run_ours(args, dist: Dist):
 
     # ---- the same step with the mixed-precision solver (FP32 inner PCG with
     # FP64 reliable updates, the FP64 stopping test)
-    mixed_ms, minfo = [], None
+    mixed_ms, mixed_pcg_ms, minfo = [], [], None
     for k in range(args.warmup + args.steps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         e0.record(ext)
         ctx.assemble_resident()
+        e2.record(ext)
         minfo = ctx.solve_resident(precision=E.PREC_MIXED, tol=TOL, maxit=MAXIT)
         e1.record(ext)
         torch.cuda.synchronize(dev)
         if k >= args.warmup:
             mixed_ms.append(e0.elapsed_time(e1))
+            mixed_pcg_ms.append(e2.elapsed_time(e1))
     xm = ctx.solution()
     spmv32_ms = time_spmv(E.PREC_MIXED)
     spmv32_bytes = 8 * nad + 16 * neq
@@ -285,6 +287,8 @@ def run_ours(args, dist: Dist):
                          "fp64_pipe_frac_ncu": profiled("fp64_pipe_frac")},
             "mixed": {"ms_per_step": mixed_step, "solves_per_s": n * 1000.0 / mixed_step,
                       "speedup_vs_fp64": ms_step / mixed_step,
+                      "pcg_ms": statistics.median(mixed_pcg_ms),
+                      "pcg_speedup_vs_fp64": pcg_ms / statistics.median(mixed_pcg_ms),
                       "pcg_iters": minfo["iters"], "refinements": minfo["refinements"],
                       "rel_err_vs_fp64": float(np.abs(xm - x64).max() / np.abs(x64).max()),
                       "norm_m_r": minfo["norm_m_r"], "conv": minfo["conv"],
@@ -336,6 +340,162 @@ def run_spmv_only(args):
     return {"mode": "spmv", "precision": args.precision, "neq": neq, "nad": nad, "spmv_ms": ms,
             "spmv_gbs": byts / (ms * 1e-3) / 1e9, "frac": byts / (ms * 1e-3) / 1e9 / peak,
             "peak": peak, "peak_kind": kind}
+
+
+def run_block(args):
+    """Batched load cases (the 96x96x48 HEXA8 plate, 16 cases of N(0,1) top-face
+    forces, tol 1e-8): block PCG with the autotuned width (FP32 inner, FP64
+    replacements) against single-RHS FP64 PCG solves, both on the device."""
+    import torch
+
+    import elastic_gb300 as E
+    from elastic_gb300 import meshgen as M
+
+    mesh, F = M.plate_hexa8_96(16)
+    ctx = E.Context(device=0)
+    ctx.set_mesh(mesh)
+    neq, nad, _ = ctx.build_structure(True)
+    st = ctx.structure()
+    B = np.zeros((neq, 16), order="F")
+    free = st.id > 0
+    for c in range(16):
+        B[st.id[free] - 1, c] = F[c][free]
+    ctx.assemble(None, None)
+    width, tt = ctx.autotune_block(E.PREC_MIXED, remeasure=True)
+    dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
+    dX = torch.zeros_like(dB)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=0)
+    times = []
+    for k in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        infos = ctx.solve_block_device(dB.data_ptr(), dX.data_ptr(), 16,
+                                       precision=E.PREC_MIXED, tol=TOL, maxit=MAXIT)
+        e1.record(ext)
+        torch.cuda.synchronize()
+        if k >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+    X = dX.cpu().numpy().T
+    ms = statistics.median(times)
+    # single-RHS FP64 PCG on two of the cases, timed the same way
+    single = []
+    for c in range(2):
+        ctx.solve(B[:, c], tol=TOL, maxit=MAXIT)  # warm
+        t = time.perf_counter()
+        x, info = ctx.solve(B[:, c], tol=TOL, maxit=MAXIT)
+        single.append((time.perf_counter() - t) * 1000.0)
+        err = float(np.abs(x - X[:, c]).max() / np.abs(x).max())
+    its = [i["iters"] for i in infos]
+    ctx.close()
+    single_ms = statistics.mean(single)
+    return {"mode": "block", "workload": "HEXA8 plate 96x96x48, 16 load cases, tol 1e-8",
+            "neq": neq, "nad": nad, "block_width": width,
+            "spmm32_us_by_width": dict(zip(["1", "2", "4", "8", "16"], np.round(tt, 1).tolist())),
+            "ms_16_cases": ms, "ms_per_case": ms / 16, "iters_min_max": [min(its), max(its)],
+            "replacements": infos[0]["refinements"],
+            "single_fp64_ms_per_case": single_ms,
+            "speedup_per_case_vs_single_fp64": single_ms / (ms / 16),
+            "rel_err_vs_fp64_case0": err}
+
+
+def run_serve(args):
+    """The served stream: N requests (box meshes of the four element types,
+    2k-2M dofs log-uniform, 1-8 load cases, tol 1e-8) with Poisson arrivals at
+    1.5x the sequential service rate, through the solve server with a 150 GB
+    admission budget, against the same stream solved one request at a time
+    with plain FP64 PCG (library single solves; its latencies follow from the
+    measured service times and the arrival times, a FIFO queue)."""
+    import threading
+
+    import elastic_gb300 as E
+    from elastic_gb300 import meshgen as M
+
+    rng = np.random.default_rng(20261203)
+    n = args.requests
+    reqs = [M.serving_request(rng, dof_max=args.max_dof) for _ in range(n)]
+    cases = sum(F.shape[0] for _, F in reqs)
+    # ---- sequential plain FP64 (service time per request, back to back)
+    service, ref_u = [], {}
+    for i, (m, F) in enumerate(reqs):
+        t0 = time.perf_counter()
+        ctx = E.Context(device=0)
+        ctx.set_mesh(m)
+        ctx.build_structure(True)
+        st = ctx.structure()
+        ctx.assemble(None, None)
+        free = st.id > 0
+        us = []
+        for k in range(F.shape[0]):
+            b = np.zeros(st.neq)
+            b[st.id[free] - 1] = F[k][free]
+            x, _ = ctx.solve(b, tol=TOL, maxit=MAXIT)
+            if i % 8 == 0:
+                u = np.zeros_like(F[k])
+                u[free] = x[st.id[free] - 1]
+                us.append(u)
+        ctx.close()
+        service.append(time.perf_counter() - t0)
+        if us:
+            ref_u[i] = np.array(us)
+    rate = 1.5 / statistics.mean(service)
+    arrivals = np.cumsum(np.random.default_rng(7).exponential(1.0 / rate, n))
+    arrivals -= arrivals[0]
+    t, lat_seq = 0.0, []
+    for a, sv in zip(arrivals, service):
+        t = max(t, a) + sv
+        lat_seq.append(t - a)
+    seq_span = t
+    # ---- served
+    srv = E.Server(device=0, hbm_budget=int(150e9), prep_threads=len(os.sched_getaffinity(0)))
+    tickets = [None] * n
+    t_start = time.perf_counter() + 0.5
+
+    def submitter():
+        for i, (m, F) in enumerate(reqs):
+            dt = t_start + arrivals[i] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            tickets[i] = (srv.submit(m, F, tol=TOL, maxit=MAXIT), time.perf_counter())
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    lat, done_at, errs, bad = [], [], [], 0
+    for i in range(n):
+        while tickets[i] is None:
+            time.sleep(0.001)
+        tk, t_sub = tickets[i]
+        U, infos, latency, status = srv.wait(tk, timeout=3600)
+        bad += status != 0
+        lat.append(latency)
+        done_at.append(t_sub - t_start + latency)
+        if i in ref_u:
+            errs.append(float(np.abs(U - ref_u[i]).max() / max(np.abs(ref_u[i]).max(), 1e-300)))
+    th.join()
+    stats = srv.stats()
+    # the same requests all at once (a closed batch): the server's capacity
+    t0 = time.perf_counter()
+    tks = [srv.submit(m, F, tol=TOL, maxit=MAXIT) for m, F in reqs]
+    for tk in tks:
+        srv.wait(tk, timeout=3600)
+    sat_span = time.perf_counter() - t0
+    srv.close()
+    span = max(done_at)
+    pct = lambda v, q: float(np.percentile(np.array(v), q))
+    return {"mode": "serve", "requests": n, "load_cases": cases,
+            "dof_range": [2e3, args.max_dof], "arrival_rate_per_s": rate,
+            "served": {"solves_per_s": cases / span, "requests_per_s": n / span,
+                       "p50_latency_s": pct(lat, 50), "p99_latency_s": pct(lat, 99),
+                       "span_s": span, "failed": int(bad),
+                       "peak_device_bytes": stats["peak_bytes"],
+                       "peak_load_cases_in_pack": stats["peak_slots"],
+                       "packed_iterations": stats["iterations"],
+                       "all_at_once_solves_per_s": cases / sat_span},
+            "sequential_fp64": {"solves_per_s": cases / seq_span, "requests_per_s": n / seq_span,
+                                "p50_latency_s": pct(lat_seq, 50),
+                                "p99_latency_s": pct(lat_seq, 99), "span_s": seq_span,
+                                "mean_service_s": statistics.mean(service)},
+            "max_rel_diff_vs_sequential_sample": max(errs) if errs else None}
 
 
 # ------------------------------------------------------------------ CPU side
@@ -417,8 +577,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--mode", choices=["full", "spmv"], default="full",
-                    help="spmv: only the SpMV of the workload (for profiling)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="full mode: skip the block and serve sub-benchmarks")
+    ap.add_argument("--mode", choices=["full", "spmv", "block", "serve"], default="full",
+                    help="spmv: only the SpMV of the workload (for profiling); block: 16 load "
+                         "cases on the 96x96x48 plate; serve: the served request stream")
+    ap.add_argument("--requests", type=int, default=512, help="serve: requests in the stream")
+    ap.add_argument("--max-dof", type=float, default=2e6, help="serve: largest request")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
                     help="solver precision (mixed: FP32 inner PCG + FP64 refinement)")
     args = ap.parse_args()
@@ -429,8 +594,22 @@ def main():
             out = run_reference(args, dist)
         elif args.mode == "spmv":
             out = run_spmv_only(args)
+        elif args.mode == "block":
+            out = run_block(args)
+        elif args.mode == "serve":
+            out = run_serve(args)
         else:
             out = run_ours(args, dist)
+            if out is not None and dist.ws == 1 and not args.no_extras:
+                # the other two headline workloads, at their own sizes (block) and
+                # on a shortened stream (serve: 64 requests up to 2e5 dofs; the
+                # full 512-request stream is --mode serve)
+                blk = argparse.Namespace(**vars(args))
+                blk.steps, blk.warmup = 3, 3
+                out["block"] = run_block(blk)
+                srv = argparse.Namespace(**vars(args))
+                srv.requests, srv.max_dof = 64, 2e5
+                out["serve"] = run_serve(srv)
     finally:
         dist.close()
     if out is not None and dist.rank == 0:
