@@ -367,7 +367,15 @@ void post_diagnostics(elx_ctx *c) {
   c->launches += 1;
   ELX_CUDA(cudaMemcpyAsync(c->h_diag, c->diag.p, 4 * sizeof(double), cudaMemcpyDeviceToHost,
                            c->stream));
+  // a bounded device wait that gave up (pipelined SpMV) leaves its code here
+  ELX_CUDA(cudaMemcpyAsync(c->h_flags + 2, c->flags.as<int32_t>() + 2, sizeof(int32_t),
+                           cudaMemcpyDeviceToHost, c->stream));
   c->sync();
+  if (c->h_flags[2] != 0) {
+    ELX_CUDA(cudaMemsetAsync(c->flags.as<int32_t>() + 2, 0, sizeof(int32_t), c->stream));
+    c->sync();
+    throw Error{ELX_ERR_TIMEOUT, "a bounded device wait of the SpMV pipeline gave up"};
+  }
 }
 
 void set_scalars(elx_ctx *c, double tol, int maxit) {

@@ -16,10 +16,13 @@
 // products are always accumulated in double.  Reductions are two-level with a
 // fixed grid (elx_reduce.cuh), so results are deterministic.
 //
-// Mixed precision (refinement kernels below): with x = 0 and r = b in FP64,
-// repeat { r32 = r; solve K32 d = r32 by FP32 PCG to a loose tolerance;
-// x += d in FP64; r = b - K x with the FP64 SpMV } until the reference's
-// test ||r||_M < tol ||b||_M holds in FP64.
+// Mixed precision (rel_* kernels below): FP32 CG with reliable updates.  The
+// FP32 iteration (FP32 SpMV, update, direction) carries the recurrence; the
+// solution is accumulated in FP64 (x_hi += x_lo at each replacement), and
+// whenever the FP32 residual has dropped tenfold since the last replacement
+// (checked every few iterations) it is replaced by the FP64 residual
+// b - K x_hi; the stopping test is the reference's ||r||_M < tol ||b||_M on
+// that FP64 residual.
 #include "elx_krylov.h"
 #include "elx_reduce.cuh"
 
