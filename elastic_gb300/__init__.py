@@ -64,13 +64,14 @@ class Info(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("device", C.c_int32), ("prep_threads", C.c_int32), ("hbm_budget", C.c_int64),
-                ("poll_steps", C.c_int32), ("max_slots", C.c_int32)]
+                ("poll_steps", C.c_int32), ("max_slots", C.c_int32), ("large_dofs", C.c_int32),
+                ("large_mode", C.c_int32), ("large_workers", C.c_int32)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("peak_bytes", C.c_int64),
                 ("resident_bytes", C.c_int64), ("peak_slots", C.c_int64),
-                ("iterations", C.c_int64)]
+                ("iterations", C.c_int64), ("large_solved", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -497,10 +498,15 @@ class Server:
     nodal displacements; requests are batched continuously on the GPU."""
 
     def __init__(self, device: int = 0, hbm_budget: int = 0, prep_threads: int = 4,
-                 poll_steps: int = 8, max_slots: int = 4096):
+                 poll_steps: int = 8, max_slots: int = 4096, large_dofs: int = 0,
+                 large_mode: int = 0, large_workers: int = 0):
+        """large_dofs: requests with at least this many equations are solved
+        whole by the block PCG (0: library default 100000); large_mode 0 auto
+        (mixed in 3-D, FP64 in 2-D), 1 FP64, 2 mixed, -1 pack everything."""
         self._L = load()
         self._h = _VP()
-        o = ServerOpts(device, prep_threads, hbm_budget, poll_steps, max_slots)
+        o = ServerOpts(device, prep_threads, hbm_budget, poll_steps, max_slots, large_dofs,
+                       large_mode, large_workers)
         st = self._L.elx_server_create(C.byref(self._h), C.byref(o))
         if st != OK:
             raise ElasticError(st, "server creation failed")

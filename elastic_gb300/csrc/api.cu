@@ -437,6 +437,7 @@ void pcg_mixed(elx_ctx *c, double tol, int maxit, elx_info *info) {
   init.bmb = bmb;
   init.conv = tol * std::sqrt(std::fabs(bmb));
   init.delta = 0.1;
+  init.best = std::sqrt(std::fabs(bmb));  // ||b - K 0||_M
   c->h_scal[0] = init;
   ELX_CUDA(cudaMemcpyAsync(c->scal.p, &c->h_scal[0], sizeof(init), cudaMemcpyHostToDevice,
                            c->stream));
@@ -452,6 +453,17 @@ void pcg_mixed(elx_ctx *c, double tol, int maxit, elx_info *info) {
   const double secs =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (!last.done) last.status = ELX_ERR_NO_CONVERGENCE;
+  if (last.failed) {
+    // the FP32 iteration diverged or stalled (an FP32 matrix too
+    // ill-conditioned for it): the case is solved in FP64 from scratch;
+    // refinements = -1 marks the fallback, inner_iters the FP32 work spent
+    pcg64(c, tol, maxit, info);
+    if (info) {
+      info->refinements = -1;
+      info->inner_iters = last.iters;
+    }
+    return;
+  }
   fill_info(c, info, last, secs);
   if (info) {
     info->refinements = last.nupdates;
@@ -720,6 +732,8 @@ void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int
   }
   const double per_iter = mixed ? 3 + 3.0 / kReplaceEvery : 3;
   int status = ELX_OK;
+  std::vector<int> fallback;  // mixed columns to solve again in FP64
+  std::vector<int> fallback_fp32_iters;
   for (int c0 = 0; c0 < nrhs; c0 += w) {
     const int nc = std::min(w, nrhs - c0);
     // b columns -> column-major staging (zero columns pad a short block)
@@ -767,6 +781,11 @@ void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int
     for (int j = 0; j < nc; j++) {
       const elx::ColScalars &s = cs[j];
       int st = s.done ? s.status : ELX_ERR_NO_CONVERGENCE;
+      if (mixed && s.failed) {
+        fallback.push_back(c0 + j);
+        fallback_fp32_iters.push_back(s.iters);
+        st = ELX_OK;  // decided by the FP64 solve below
+      }
       if (st != ELX_OK && status == ELX_OK) status = st;
       if (!infos) continue;
       elx_info &in = infos[c0 + j];
@@ -782,6 +801,38 @@ void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int
       in.refinements = mixed ? s.nupdates : 0;
       in.inner_iters = mixed ? s.iters : 0;
     }
+  }
+  if (!fallback.empty()) {
+    // columns whose FP32 iteration diverged or stalled: FP64 PCG one by one
+    // (the context's assembled b is kept aside meanwhile)
+    ELX_CUDA(cudaMemcpyAsync(c->bk_z.p, c->b.p, n * 8, cudaMemcpyDeviceToDevice, c->stream));
+    for (size_t f = 0; f < fallback.size(); f++) {
+      const int col = fallback[f];
+      ELX_CUDA(cudaMemcpyAsync(c->b.p, b + (size_t)col * n, n * 8,
+                               device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               c->stream));
+      elx_info in{};
+      int st = ELX_OK;
+      try {
+        pcg64(c, tol, maxit, &in);
+      } catch (const Error &e) {
+        if (e.code != ELX_ERR_NO_CONVERGENCE) throw;
+        st = e.code;
+      }
+      ELX_CUDA(cudaMemcpyAsync(x + (size_t)col * n, c->xs.p, n * 8,
+                               device_ptrs ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                               c->stream));
+      c->sync();
+      if (st != ELX_OK && status == ELX_OK) status = st;
+      if (infos) {
+        in.status = st;
+        in.refinements = -1;
+        in.inner_iters = fallback_fp32_iters[f];
+        infos[col] = in;
+      }
+    }
+    ELX_CUDA(cudaMemcpyAsync(c->b.p, c->bk_z.p, n * 8, cudaMemcpyDeviceToDevice, c->stream));
+    c->sync();
   }
   if (status != ELX_OK) throw Error{status, "block PCG: a load case did not converge"};
 }

@@ -413,6 +413,7 @@ brel_start_kernel(int n, const double *__restrict__ b, const double *__restrict_
     s.d = d;
     s.conv = hdr->tol * sqrt(fabs(bmb));
     s.rmax = sqrt(fabs(d));
+    s.best = sqrt(fabs(bmb));
     if (bmb == 0.0) s.done = 1;
     if (hdr->maxit <= 0 && !s.done) {
       s.done = 1;
@@ -485,7 +486,8 @@ brel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__
         const double rn = sqrt(fabs(tot));
         s.beta = tot / s.d;
         s.d = tot;
-        if (rn < hdr->delta * s.rmax || rn < s.conv || s.iters >= hdr->maxit) {
+        if (rn < hdr->delta * s.rmax || rn < s.conv || s.iters >= hdr->maxit ||
+            s.iters - s.last_rep >= kMixedCheckEvery) {
           s.update = 1;
           hdr->any_update = 1;
         }
@@ -543,16 +545,32 @@ brel_residual_kernel(int n, const double *__restrict__ b, const double *__restri
   if (threadIdx.x < W) {
     ColScalars &s = cols[threadIdx.x];
     if (!s.done) {
+      // a column replaced with the others (not by its own request) is not
+      // held to the halving test, only to the divergence test
+      const bool own = s.update != 0;
+      const double rt = sqrt(fabs(tot));
       s.update = 0;
       s.nupdates += 1;
-      if (sqrt(fabs(tot)) < s.conv) {
+      if (own) s.last_rep = s.iters;
+      if (rt < s.conv) {
         s.done = 1;
-      } else if (s.iters >= hdr->maxit || !(tot == tot)) {
+      } else if (!(tot == tot) || rt > kMixedDiverge * s.best) {
+        s.done = 1;
+        s.status = ELX_ERR_NO_CONVERGENCE;
+        s.failed = 1;
+      } else if (s.iters >= hdr->maxit) {
         s.done = 1;
         s.status = ELX_ERR_NO_CONVERGENCE;
       } else {
+        if (own) s.stall = rt < 0.5 * s.best ? 0 : s.stall + 1;
+        s.best = fmin(s.best, rt);
+        if (s.stall >= kMixedStall) {
+          s.done = 1;
+          s.status = ELX_ERR_NO_CONVERGENCE;
+          s.failed = 1;
+        }
         s.d = tot;
-        s.rmax = sqrt(fabs(tot));
+        s.rmax = rt;
       }
     }
   }

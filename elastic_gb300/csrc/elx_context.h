@@ -163,6 +163,9 @@ void upload_structure(elx_ctx *c, bool prederived = false);
 void assemble_resident(elx_ctx *c);
 void build_preconditioner(elx_ctx *c);
 void release_block(elx_ctx *c);
+// Block PCG of nrhs load cases (api.cu); b, x column-major neq x nrhs.
+void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int width,
+                 const double *b, double *x, elx_info *infos, bool device_ptrs);
 void check_mesh(int32_t ndm, int32_t ndf, int32_t nen, int32_t numel, int32_t nnode,
                 const int32_t *ix, const int32_t *ie, int32_t numat, int32_t prop);
 void fill_mesh(elx::Mesh &m, int32_t ndm, int32_t ndf, int32_t nen, int32_t numel,

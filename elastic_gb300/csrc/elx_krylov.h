@@ -22,7 +22,25 @@ struct PcgScalars {
   int32_t status;
   int32_t update;    // mixed precision: a residual replacement is due
   int32_t nupdates;  // mixed precision: replacements so far
+  // mixed precision: progress watch of the FP64 residual at replacements
+  double best;       // smallest ||b - K x||_M seen so far
+  int32_t last_rep;  // iteration of the last replacement
+  int32_t stall;     // own replacements in a row that did not halve `best`
+  int32_t failed;    // the FP32 iteration diverged or stalled: solve in FP64
+  int32_t pad_;
 };
+
+// Progress watch of the mixed-precision solvers.  A matrix rounded to FP32
+// can lose definiteness when K is ill-conditioned (cond(K) near 1/eps32, as
+// in 2-D meshes of 10^6 dofs): the FP32 recurrence then stalls or diverges.
+// At every replacement the FP64 residual is compared with the best so far;
+// a residual kMixedDiverge times the best, or kMixedStall own replacements
+// in a row that do not halve it, end the FP32 iteration (`failed`), and the
+// host solves the case in FP64.  A replacement is forced every
+// kMixedCheckEvery iterations so that a stall is seen.
+constexpr int kMixedCheckEvery = 512;
+constexpr double kMixedDiverge = 100.0;
+constexpr int kMixedStall = 4;
 
 // State of one GMRES(k) solve, resident in device memory (the small dense
 // arrays live in a separate buffer of gmres_array_doubles(k) doubles).
@@ -46,6 +64,8 @@ struct GmresState {
 struct ColScalars {
   double d, alpha, beta, pq, rmax, conv, bmb;
   int32_t iters, done, status, update, nupdates, pad;
+  double best;  // progress watch, as in PcgScalars
+  int32_t last_rep, stall, failed, pad2;
 };
 struct BlockHeader {
   double tol;      // (input)

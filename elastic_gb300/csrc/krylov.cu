@@ -340,7 +340,9 @@ rel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__ 
     }
     sc->beta = di / sc->d;
     sc->d = di;
-    if (rn < sc->delta * sc->rmax || rn < sc->conv || it >= sc->maxit) sc->update = 1;
+    if (rn < sc->delta * sc->rmax || rn < sc->conv || it >= sc->maxit ||
+        it - sc->last_rep >= kMixedCheckEvery)
+      sc->update = 1;
   }
 }
 
@@ -376,17 +378,29 @@ rel_residual_kernel(int n, const double *__restrict__ b, const double *__restric
   double tot[1];
   gather_partials<1>(tot, partials, counter);
   if (threadIdx.x == 0) {
-    const double di = tot[0];
+    const double di = tot[0], rt = sqrt(fabs(di));
     sc->update = 0;
     sc->nupdates += 1;
-    if (sqrt(fabs(di)) < sc->conv) {
+    sc->last_rep = sc->iters;
+    if (rt < sc->conv) {
       sc->done = 1;
-    } else if (sc->iters >= sc->maxit || !(di == di)) {
+    } else if (!(di == di) || rt > kMixedDiverge * sc->best) {
+      sc->done = 1;
+      sc->status = ELX_ERR_NO_CONVERGENCE;
+      sc->failed = 1;
+    } else if (sc->iters >= sc->maxit) {
       sc->done = 1;
       sc->status = ELX_ERR_NO_CONVERGENCE;
     } else {
+      sc->stall = rt < 0.5 * sc->best ? 0 : sc->stall + 1;
+      sc->best = fmin(sc->best, rt);
+      if (sc->stall >= kMixedStall) {
+        sc->done = 1;
+        sc->status = ELX_ERR_NO_CONVERGENCE;
+        sc->failed = 1;
+      }
       sc->d = di;
-      sc->rmax = sqrt(fabs(di));
+      sc->rmax = rt;
     }
   }
 }

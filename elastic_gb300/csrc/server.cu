@@ -246,6 +246,7 @@ struct SrvRequest {
   int64_t need_bytes = 0;
   int64_t charged = 0;  // bytes counted against the budget while resident
   bool counted = false;
+  bool large = false;   // solved whole on its own stream (block PCG), not packed
   // device state
   elx_ctx *ctx = nullptr;
   DBuf vecs;  // b (nrhs x neq), then per load case x, r, p, q
@@ -264,6 +265,9 @@ struct elx_server {
   int64_t budget = 0;
   int poll_steps = 8;
   int max_slots = 4096;
+  int large_dofs = 100000;  // requests with at least this many equations ...
+  int large_mode = 0;       // ... 0: auto (mixed in 3-D, FP64 in 2-D), 1: FP64, 2: mixed,
+                            // -1: packed like the others
   cudaStream_t stream = nullptr;
 
   std::mutex mu;
@@ -272,8 +276,10 @@ struct elx_server {
   std::map<int64_t, std::shared_ptr<SrvRequest>> all;
   int64_t next_ticket = 1;
   bool stopping = false;
-  std::vector<std::thread> prep_threads;
+  std::vector<std::thread> prep_threads, large_threads;
   std::thread admit_thread, loop_thread;
+  std::condition_variable cv_large;
+  std::deque<std::shared_ptr<SrvRequest>> large_ready;
   std::string fatal;
 
   // shared under mu: admitted requests ready to join, free slot indices,
@@ -293,7 +299,8 @@ struct elx_server {
   cudaEvent_t ev_poll = nullptr;
 
   // statistics
-  std::atomic<int64_t> submitted{0}, completed{0}, peak_used{0}, peak_slots{0}, iterations{0};
+  std::atomic<int64_t> submitted{0}, completed{0}, peak_used{0}, peak_slots{0}, iterations{0},
+      large_solved{0};
 };
 
 namespace {
@@ -317,7 +324,17 @@ int64_t estimate_bytes(const SrvRequest &q) {
   b += 8 * s.nnzb * s.bsize * s.bsize;                 // block values
   b += 8 * n + 8 * nad;                                // ad, al
   b += 8 * (int64_t)(m.ndf * m.nnode) + 8 * 8 * n;     // u, b0, b, x, r, p, q, m, z
-  b += 5 * 8 * n * q.nrhs;                             // per load case
+  if (q.large) {
+    // block PCG of up to 16 columns: b, x in the request's buffer; block
+    // multi-vectors (7 FP64, 4 FP32 per column), FP32 blocks and vectors
+    int w = 1;
+    while (w < q.nrhs && w < 16) w *= 2;
+    b += 2 * 8 * n * q.nrhs + 7 * 8 * n * w + 4 * 4 * n * w;
+    b += 4 * s.nnzb * s.bsize * s.bsize + 5 * 4 * n;
+    b += 8 * 2 * 16 * 1216 + (64 << 10);
+  } else {
+    b += 5 * 8 * n * q.nrhs;                           // per load case
+  }
   b += 160 << 10;                                      // scalars, partials, padding
   return b;
 }
@@ -347,7 +364,6 @@ void prep_request(SrvRequest &q) {
       if (s.id[j] > 0) q.b0[(size_t)k * s.neq + s.id[j] - 1] = q.f[k * nd + j];
   q.f.clear();
   q.f.shrink_to_fit();
-  q.need_bytes = estimate_bytes(q);
 }
 
 void finish(elx_server *sv, const std::shared_ptr<SrvRequest> &q) {
@@ -376,6 +392,8 @@ void prep_worker(elx_server *sv) {
     }
     try {
       prep_request(*q);
+      q->large = sv->large_mode >= 0 && q->s.neq >= sv->large_dofs;
+      q->need_bytes = estimate_bytes(*q);
       std::lock_guard<std::mutex> lk(sv->mu);
       sv->prepared.push_back(q);
     } catch (const Error &e) {
@@ -430,6 +448,20 @@ void admit(elx_server *sv, SrvRequest &q) {
   assemble_resident(c);  // u = 0, b0 = 0: K only (the loads are the slots' b)
   build_preconditioner(c);
   const size_t n = (size_t)c->s.neq;
+  if (q.large) {
+    // b and x of all load cases (column-major) for the request's block solve
+    c->alloc(q.vecs, 2 * n * q.nrhs * 8);
+    ELX_CUDA(cudaMemcpyAsync(q.vecs.p, q.b0.data(), n * q.nrhs * 8, cudaMemcpyHostToDevice,
+                             c->stream));
+    ELX_CUDA(cudaEventCreateWithFlags(&q.ready, cudaEventDisableTiming));
+    ELX_CUDA(cudaEventRecord(q.ready, c->stream));
+    ELX_CUDA(cudaEventSynchronize(q.ready));
+    q.b0.clear();
+    q.b0.shrink_to_fit();
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->peak_used = std::max<int64_t>(sv->peak_used.load(), sv->used);
+    return;  // the estimate stays charged: the block buffers come with the solve
+  }
   c->alloc(q.vecs, 5 * n * q.nrhs * 8);
   ELX_CUDA(cudaMemcpyAsync(q.vecs.p, q.b0.data(), n * q.nrhs * 8, cudaMemcpyHostToDevice,
                            c->stream));
@@ -504,18 +536,19 @@ void admit_loop(elx_server *sv) {
           if (sv->prepared.empty()) return false;
           const auto &h = sv->prepared.front();
           const bool fits_mem = sv->budget <= 0 || sv->used + h->need_bytes <= sv->budget;
-          const bool fits_slots = (int)sv->slot_free.size() >= h->nrhs;
+          const bool fits_slots = h->large || (int)sv->slot_free.size() >= h->nrhs;
           const bool idle = sv->resident == 0;
-          return (fits_mem && fits_slots) || (idle && (!fits_mem || h->nrhs > sv->max_slots));
+          return (fits_mem && fits_slots) ||
+                 (idle && (!fits_mem || (!h->large && h->nrhs > sv->max_slots)));
         });
         if (sv->stopping) return;
         q = sv->prepared.front();
         sv->prepared.pop_front();
         const bool fits_mem = sv->budget <= 0 || sv->used + q->need_bytes <= sv->budget;
-        if (!fits_mem || q->nrhs > sv->max_slots) {
+        if (!fits_mem || (!q->large && q->nrhs > sv->max_slots)) {
           reject = true;
         } else {
-          for (int k = 0; k < q->nrhs; k++) {
+          for (int k = 0; !q->large && k < q->nrhs; k++) {
             q->slots.push_back(sv->slot_free.back());
             sv->slot_free.pop_back();
           }
@@ -536,9 +569,10 @@ void admit_loop(elx_server *sv) {
         admit(sv, *q);
         {
           std::lock_guard<std::mutex> lk(sv->mu);
-          sv->joinable.push_back(q);
+          (q->large ? sv->large_ready : sv->joinable).push_back(q);
         }
         sv->cv_admit.notify_all();
+        sv->cv_large.notify_all();
       } catch (const Error &e) {
         q->status = e.code;
         q->err = e.msg;
@@ -553,6 +587,67 @@ void admit_loop(elx_server *sv) {
   }
   sv->cv_done.notify_all();
   sv->cv_admit.notify_all();
+}
+
+// Large requests: each solved whole on its context's stream by the block PCG
+// (all its load cases over one matrix read per iteration; width fixed by the
+// number of load cases, so the result does not depend on what else runs),
+// several at once on different streams next to the pack.
+void large_loop(elx_server *sv) {
+  for (;;) {
+    std::shared_ptr<SrvRequest> q;
+    {
+      std::unique_lock<std::mutex> lk(sv->mu);
+      sv->cv_large.wait(lk, [&] { return sv->stopping || !sv->large_ready.empty(); });
+      if (sv->stopping) return;
+      q = sv->large_ready.front();
+      sv->large_ready.pop_front();
+    }
+    try {
+      ELX_CUDA(cudaSetDevice(sv->device));
+      elx_ctx *c = q->ctx;
+      const size_t n = (size_t)c->s.neq;
+      int w = 1;
+      while (w < q->nrhs && w < 16) w *= 2;
+      const double *b = q->vecs.as<double>();
+      double *x = q->vecs.as<double>() + n * q->nrhs;
+      q->infos.assign(q->nrhs, elx_info{});
+      try {
+        // auto (0): mixed in 3-D; FP64 in 2-D, where the FP32 iteration needs
+        // about twice the FP64 iterations and diverges above ~3e5 dofs (2-D
+        // plane-stress strips of 58k / 141k / 361k dofs: 2.0x / 3.2x the
+        // FP64 time, then an FP64 fallback)
+        const bool mixed = sv->large_mode == 2 || (sv->large_mode == 0 && c->mesh.ndm == 3);
+        solve_block(c, q->nrhs, mixed ? ELX_PREC_MIXED : ELX_PREC_FP64, q->tol, q->maxit, w, b, x,
+                    q->infos.data(), true);
+      } catch (const Error &e) {
+        if (e.code != ELX_ERR_NO_CONVERGENCE) throw;
+        q->status = e.code;
+        q->err = e.msg;
+      }
+      std::vector<double> xh(n * q->nrhs);
+      ELX_CUDA(cudaMemcpyAsync(xh.data(), x, n * q->nrhs * 8, cudaMemcpyDeviceToHost, c->stream));
+      ELX_CUDA(cudaStreamSynchronize(c->stream));
+      const size_t nd = (size_t)c->mesh.ndf * c->mesh.nnode;
+      q->u.assign(nd * q->nrhs, 0.0);
+      for (int k = 0; k < q->nrhs; k++)
+        for (size_t j = 0; j < nd; j++) {
+          const int e = c->s.id[j];
+          q->u[k * nd + j] = e > 0 ? xh[(size_t)k * n + e - 1] : 0.0;
+        }
+      {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->peak_used = std::max<int64_t>(sv->peak_used.load(), sv->used);
+      }
+      sv->large_solved++;
+    } catch (const Error &e) {
+      q->status = e.code;
+      q->err = e.msg;
+    }
+    q->t_done = now_s();
+    release_request(sv, *q);
+    finish(sv, q);
+  }
 }
 
 // The pack: joins admitted requests, runs poll_steps packed PCG iterations
@@ -666,13 +761,16 @@ int elx_server_create(elx_server **out, const elx_server_opts *opts) {
   *out = nullptr;
   elx_server *sv = new (std::nothrow) elx_server();
   if (!sv) return ELX_ERR_OOM;
-  int nthreads = 4;
+  int nthreads = 4, nlarge = 2;
   if (opts) {
     sv->device = opts->device;
     sv->budget = opts->hbm_budget;
     if (opts->poll_steps > 0) sv->poll_steps = opts->poll_steps;
     if (opts->max_slots > 0) sv->max_slots = opts->max_slots;
     if (opts->prep_threads > 0) nthreads = opts->prep_threads;
+    if (opts->large_dofs > 0) sv->large_dofs = opts->large_dofs;
+    sv->large_mode = opts->large_mode;
+    if (opts->large_workers > 0) nlarge = opts->large_workers;
   }
   const cudaError_t e1 = cudaSetDevice(sv->device);
   cudaError_t e = e1;
@@ -693,6 +791,7 @@ int elx_server_create(elx_server **out, const elx_server_opts *opts) {
   for (int i = sv->max_slots - 1; i >= 0; i--) sv->slot_free.push_back(i);
   for (int i = 0; i < nthreads; i++) sv->prep_threads.emplace_back(prep_worker, sv);
   sv->admit_thread = std::thread(admit_loop, sv);
+  for (int i = 0; i < nlarge; i++) sv->large_threads.emplace_back(large_loop, sv);
   sv->loop_thread = std::thread(gpu_loop, sv);
   *out = sv;
   return ELX_OK;
@@ -707,13 +806,17 @@ void elx_server_destroy(elx_server *sv) {
   sv->cv_prep.notify_all();
   sv->cv_admit.notify_all();
   sv->cv_done.notify_all();
+  sv->cv_large.notify_all();
   for (auto &t : sv->prep_threads)
+    if (t.joinable()) t.join();
+  for (auto &t : sv->large_threads)
     if (t.joinable()) t.join();
   if (sv->admit_thread.joinable()) sv->admit_thread.join();
   if (sv->loop_thread.joinable()) sv->loop_thread.join();
   cudaSetDevice(sv->device);
   for (auto &q : sv->active) release_request(sv, *q);
   for (auto &q : sv->joinable) release_request(sv, *q);
+  for (auto &q : sv->large_ready) release_request(sv, *q);
   if (sv->stream) cudaStreamSynchronize(sv->stream);
   if (sv->d_sc) cudaFree(sv->d_sc);
   if (sv->d_desc) cudaFree(sv->d_desc);
@@ -794,6 +897,7 @@ int elx_server_get_stats(elx_server *sv, elx_server_stats *st) {
   st->peak_bytes = sv->peak_used;
   st->peak_slots = sv->peak_slots;
   st->iterations = sv->iterations;
+  st->large_solved = sv->large_solved;
   {
     std::lock_guard<std::mutex> lk(sv->mu);
     st->resident_bytes = sv->used;

@@ -78,7 +78,9 @@ typedef struct elx_info {
   double conv;        /* stopping threshold tol * ||b||_M (GMRES/BiCGSTAB: 2-norm) */
   double seconds;     /* wall time of the solve on the device                */
   double mflops;      /* flop_cg(neq,nad,iters,2) / seconds (Matvec.f:1499) */
-  int32_t refinements;/* mixed precision: outer FP64 refinement steps        */
+  int32_t refinements;/* mixed precision: FP64 residual replacements; -1 when */
+                      /* the FP32 iteration diverged or stalled and the case  */
+                      /* was solved in FP64 instead                           */
   int32_t inner_iters;/* mixed precision: total FP32 inner iterations        */
 } elx_info;
 
@@ -186,7 +188,10 @@ int elx_autotune_block(elx_ctx *ctx, int32_t precision, int32_t *width, double *
  * budget; the PCG iterations of all admitted requests (every load case) run
  * as one packed set of kernels per iteration, each load case with its own
  * scalars and stopping test; requests join and leave between polls
- * (continuous batching).  A result is bitwise the same alone and in a mix. */
+ * (continuous batching).  Requests of large_dofs equations or more are
+ * instead solved whole, several at once on their own streams, by the block
+ * PCG over all their load cases (see large_mode).
+ * A result is bitwise the same alone and in a mix. */
 typedef struct elx_server elx_server;
 typedef struct elx_server_opts {
   int32_t device;
@@ -194,6 +199,13 @@ typedef struct elx_server_opts {
   int64_t hbm_budget;   /* device bytes for admitted requests (0: no limit)  */
   int32_t poll_steps;   /* PCG iterations between polls (0: 8)               */
   int32_t max_slots;    /* load cases in flight at most (0: 4096)            */
+  int32_t large_dofs;   /* requests with at least this many equations are   */
+                        /* solved whole, not packed (0: 100000)             */
+  int32_t large_mode;   /* those: block PCG, 0 auto (mixed precision in     */
+                        /* 3-D, FP64 in 2-D), 1 FP64, 2 mixed (FP32 inner,  */
+                        /* FP64 replacements and test), -1 packed like the  */
+                        /* others                                           */
+  int32_t large_workers;/* large requests solved at once (0: 2)             */
 } elx_server_opts;
 typedef struct elx_server_stats {
   int64_t submitted, completed;
@@ -201,6 +213,7 @@ typedef struct elx_server_stats {
   int64_t resident_bytes; /* bytes held now                                   */
   int64_t peak_slots;     /* most load cases in one packed iteration         */
   int64_t iterations;     /* packed iterations run                           */
+  int64_t large_solved;   /* requests solved whole (block PCG)               */
 } elx_server_stats;
 int elx_server_create(elx_server **out, const elx_server_opts *opts);
 /* Queues a request (the arrays are copied): a mesh as for elx_set_mesh,

@@ -105,3 +105,25 @@ def test_block_autotune(gpu_ctx):
         assert w in (1, 2, 4, 8, 16)
         assert np.all(t > 0)
         assert gpu_ctx.autotune_block(prec)[0] == w
+
+
+def test_mixed_falls_back_to_fp64_on_ill_conditioned_2d(gpu_ctx):
+    """A 2-D mesh of ~10^5 dofs is ill-conditioned enough for its FP32 matrix
+    to stall or diverge the FP32 iteration; the mixed solvers then solve the
+    case in FP64 (refinements = -1).  Either way the answer meets the FP64
+    stopping test and matches the FP64 solve."""
+    m = M.box2d(240, 120, 2.0, 1.0, etype=M.QUAD4_STRESS, E=1.0, nu=0.3)
+    gpu_ctx.set_mesh(m)
+    gpu_ctx.build_structure(True)
+    neq = gpu_ctx.sizes()[0]
+    gpu_ctx.assemble(None, None)
+    B = np.random.default_rng(12).standard_normal((neq, 3))
+    X64, i64 = gpu_ctx.solve_block(B, precision=E.PREC_FP64, tol=1e-10, width=4)
+    Xm, im = gpu_ctx.solve_block(B, precision=E.PREC_MIXED, tol=1e-10, width=4)
+    x1, i1 = gpu_ctx.solve(B[:, 0], precision=E.PREC_MIXED, tol=1e-10, maxit=50000)
+    for c in range(3):
+        assert im[c]["status"] == 0 and im[c]["norm_m_r"] <= 3.16 * im[c]["conv"]
+        bar = 1e-9 if im[c]["refinements"] == -1 else 1e-6
+        assert rel_inf(X64[:, c], Xm[:, c]) <= bar
+    assert i1["status"] == 0 and i1["norm_m_r"] <= 3.16 * i1["conv"]
+    assert rel_inf(X64[:, 0], x1) <= (1e-9 if i1["refinements"] == -1 else 1e-6)

@@ -4,7 +4,9 @@ Bars: every load case of every request equals the oracle's FP64 PCG solution
 (pcg, Iters.f:252-524, tol 1e-10) within 1e-9 relative with iterations within
 +-2; a request's result is bitwise the same alone and in a mix; admission
 respects the HBM budget; a bad request fails alone without stopping the
-server.
+server; requests above the size threshold, solved whole by the block PCG,
+meet the same bars (FP64 block PCG: 1e-9; mixed: the FP64 stopping test and
+1e-6 of the oracle) and are bitwise the same alone and in a mix.
 """
 import numpy as np
 import pytest
@@ -98,3 +100,25 @@ def test_no_convergence_reported(built_lib):
         assert status == E.ERR_NO_CONVERGENCE
         assert all(i["iters"] == 5 for i in infos)
         assert np.isfinite(U).all()
+
+
+@pytest.mark.parametrize("mode,bar", [(2, 1e-6), (1, 1e-9)])
+def test_large_requests_solved_whole(built_lib, mode, bar):
+    reqs = _requests(11, 6)
+    with E.Server(device=0, large_dofs=1, large_mode=mode) as srv:
+        tickets = [srv.submit(m, F, tol=TOL, maxit=50000) for m, F in reqs]
+        res = [srv.wait(t, timeout=300) for t in tickets]
+        assert srv.stats()["large_solved"] == len(reqs)
+        for (m, F), (U, infos, lat, status) in zip(reqs, res):
+            assert status == 0
+            U_o, it_o = _oracle(m, F)
+            for k in range(F.shape[0]):
+                assert infos[k]["status"] == 0
+                assert infos[k]["norm_m_r"] <= 3.16 * infos[k]["conv"]
+                assert rel_inf(U_o[k], U[k]) <= bar, (m.name, k, mode)
+                if mode == 1:
+                    assert abs(infos[k]["iters"] - it_o[k]) <= 2
+        # alone: bitwise the same
+        for (m, F), (U, _, _, _) in zip(reqs[:3], res[:3]):
+            U1, _, _, st1 = srv.wait(srv.submit(m, F, tol=TOL, maxit=50000), timeout=300)
+            assert st1 == 0 and np.array_equal(U1, U)
