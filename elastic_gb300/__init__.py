@@ -136,6 +136,8 @@ def load():
         "elx_solve_block_device": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                              C.c_int32, _VP, _VP, _VP]),
         "elx_autotune_block": (C.c_int, [_VP, C.c_int32, P(C.c_int32), _VP]),
+        "elx_stress": (C.c_int, [_VP, _VP, _VP, _VP]),
+        "elx_update_resident": (C.c_int, [_VP]),
         "elx_server_create": (C.c_int, [P(_VP), P(ServerOpts)]),
         "elx_server_destroy": (None, [_VP]),
         "elx_server_submit": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
@@ -327,6 +329,17 @@ class Context:
         d["status"] = st if st != OK else d["status"]
         return x, d
 
+    def stress(self, u=None, tx0=None):
+        """tform_mec: nodal stresses (nnode, ntn) from nodal displacements u
+        (nnode, ndf; None: the resident u) and initial stresses tx0."""
+        m = self.mesh
+        ntn = 4 if m.ndm == 2 else 6
+        t = np.zeros((m.nnode, ntn))
+        uu = None if u is None else _f64(u)
+        tt = None if tx0 is None else _f64(tx0)
+        self._check(self._L.elx_stress(self._h, _ptr(uu), _ptr(tt), t.ctypes.data_as(_VP)))
+        return t
+
     def solve_block(self, B, precision=PREC_MIXED, tol=1e-8, maxit=20000, width=0,
                     raise_on_error=True):
         """Block PCG for the columns of B (neq x nrhs): returns (X, infos)."""
@@ -384,6 +397,10 @@ class Context:
         self._check(self._L.elx_solve_resident(self._h, solver, precision, tol, maxit, ngram,
                                                C.byref(info)))
         return info.as_dict()
+
+    def update_resident(self):
+        """u(id) = x on the device (update_mec without a host round trip)."""
+        self._check(self._L.elx_update_resident(self._h))
 
     def spmv_resident(self, precision=PREC_FP64, reps=1):
         self._check(self._L.elx_spmv_resident(self._h, precision, reps))

@@ -151,6 +151,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
     c->release(*v);
   release_block(c);
   c->tuned_width[0] = c->tuned_width[1] = 0;
+  for (DBuf *v : {&c->node_count, &c->tstress, &c->tx0buf}) c->release(*v);
   c->have_fp32 = false;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
@@ -967,6 +968,7 @@ void elx_destroy(elx_ctx *c) {
                   &c->ad32, &c->al32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32,
                   &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate,
                   &c->bia, &c->bja, &c->bt, &c->bval, &c->bval32,
+                  &c->node_count, &c->tstress, &c->tx0buf,
                   &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
                   &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
     c->release(*d);
@@ -1194,6 +1196,55 @@ int elx_solve(elx_ctx *c, int32_t solver, int32_t precision, double tol, int32_t
   });
 }
 
+int elx_stress(elx_ctx *c, const double *u, const double *tx0, double *t) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "stresses before the structure is set");
+    require(t != nullptr, ELX_ERR_ARG, "null t");
+    const elx::Mesh &m = c->mesh;
+    const int ntn = m.ndm == 2 ? 4 : 6;
+    const size_t nn = (size_t)m.nnode;
+    if (!c->node_count.p) {
+      // elements at each node (ic of Pform.f:400-403), once per mesh
+      std::vector<int32_t> cnt(nn, 0);
+      for (int el = 0; el < m.numel; el++)
+        for (int a = 0; a < m.nen; a++) {
+          const int no = m.ix[(size_t)el * (m.nen + 1) + a];
+          if (no > 0) cnt[no - 1]++;
+        }
+      c->upload(c->node_count, cnt.data(), cnt.size());
+      c->alloc(c->tstress, nn * ntn * 8);
+      c->sync();
+    }
+    if (u)
+      ELX_CUDA(cudaMemcpyAsync(c->u.p, u, (size_t)m.ndf * nn * 8, cudaMemcpyHostToDevice,
+                               c->stream));
+    const double *tx0d = nullptr;
+    if (tx0) {
+      if (!c->tx0buf.p) c->alloc(c->tx0buf, nn * ntn * 8);
+      ELX_CUDA(cudaMemcpyAsync(c->tx0buf.p, tx0, nn * ntn * 8, cudaMemcpyHostToDevice,
+                               c->stream));
+      tx0d = c->tx0buf.as<double>();
+    }
+    ELX_CUDA(cudaMemsetAsync(c->tstress.p, 0, nn * ntn * 8, c->stream));
+    const int32_t big = INT_MAX;
+    int32_t *bad = c->flags.as<int32_t>();
+    ELX_CUDA(cudaMemcpyAsync(bad, &big, sizeof(big), cudaMemcpyHostToDevice, c->stream));
+    const elx::MeshDev md = c->mesh_dev();
+    for (const elx::Segment &seg : c->s.segments)
+      elx::launch_stress(md, seg, c->u.as<double>(), c->tstress.as<double>(), bad, c->stream);
+    elx::launch_stress_average(m.nnode, ntn, c->node_count.as<int32_t>(), tx0d,
+                               c->tstress.as<double>(), c->stream);
+    c->launches += (int64_t)c->s.segments.size() + 1;
+    ELX_CUDA(cudaMemcpyAsync(t, c->tstress.p, nn * ntn * 8, cudaMemcpyDeviceToHost, c->stream));
+    ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             c->stream));
+    c->sync();
+    if (c->h_flags[0] != INT_MAX)
+      throw Error{ELX_ERR_BAD_DET, "non-positive Jacobian determinant in element " +
+                                       std::to_string(c->h_flags[0])};
+  });
+}
+
 int elx_solve_block(elx_ctx *c, int32_t nrhs, int32_t precision, double tol, int32_t maxit,
                     int32_t width, const double *b, double *x, elx_info *info) {
   return guarded(c, [&] {
@@ -1229,6 +1280,15 @@ int elx_update(elx_ctx *c, const double *x, double *u) {
     const std::vector<int32_t> &id = c->s.id;
     for (size_t q = 0; q < id.size(); q++)
       if (id[q] > 0) u[q] = x[id[q] - 1];
+  });
+}
+
+int elx_update_resident(elx_ctx *c) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "set the structure first");
+    elx::launch_update((int64_t)c->mesh.ndf * c->mesh.nnode, c->eq.as<int32_t>(),
+                       c->xs.as<double>(), c->u.as<double>(), c->stream);
+    c->launches += 1;
   });
 }
 

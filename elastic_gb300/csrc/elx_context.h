@@ -45,6 +45,8 @@ struct elx_ctx {
   DBuf u, b0, b, xs, r, p, q, m, z;
   // mixed precision: FP32 inner PCG vectors and preconditioner
   DBuf m32, p32, q32, r32, x32;
+  // stress recovery: elements per node, nodal stresses, initial stresses
+  DBuf node_count, tstress, tx0buf;
   // BiCGSTAB (r0, t) and GMRES (Krylov basis, small dense arrays, state)
   DBuf r0v, tv, gbasis, garrays, gstate;
   // block PCG: multi-vectors of up to blk_cap columns, scalars, staging

@@ -184,6 +184,13 @@ void launch_tile_spmv64(const CsrcDev &k, const TileDev &t, const double *x, dou
                         double *part, int32_t *err, cudaStream_t st);
 void launch_tile_spmv32(const CsrcDev &k, const TileDev &t, const float *x, float *ytile,
                         float *part, int32_t *err, cudaStream_t st);
+// Stress recovery (stress.cu): nodal stress sums of one colour segment, then
+// the per-node average + tx0.
+void launch_stress(const MeshDev &m, const Segment &seg, const double *u, double *ts,
+                   int32_t *bad, cudaStream_t st);
+void launch_stress_average(int nnode, int ntn, const int32_t *count, const double *tx0,
+                           double *ts, cudaStream_t st);
+void launch_update(int64_t n, const int32_t *eq, const double *x, double *u, cudaStream_t st);
 void launch_demote_values(const CsrcDev &k, cudaStream_t st);
 void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
 // Node-block values from the CSRC arrays (k.bval), and their FP32 copy.

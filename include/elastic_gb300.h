@@ -235,6 +235,14 @@ int elx_server_wait(elx_server *srv, int64_t ticket, double timeout_s, double *u
 int elx_server_get_stats(elx_server *srv, elx_server_stats *stats);
 void elx_server_destroy(elx_server *srv);
 
+/* Stress recovery, tform_mec (Pform.f:258-421, called for isw = 3 at
+ * Main.f:893-901): t(ntn,nnode) = for each node the average over its
+ * elements of their stresses at the node (elmt02-07_mec isw = 3) + tx0
+ * (ntn = 4: sxx syy szz sxy in 2-D; 6: sxx syy szz sxy syz sxz in 3-D).
+ * u(ndf,nnode) the nodal displacements (NULL: the resident u of
+ * elx_set_state); tx0(ntn,nnode) initial stresses (NULL: zero). */
+int elx_stress(elx_ctx *ctx, const double *u, const double *tx0, double *t);
+
 /* update_mec (Predict.f:183-209): u(j,i) = x(id(j,i)) for free dofs. */
 int elx_update(elx_ctx *ctx, const double *x, double *u);
 
@@ -258,6 +266,11 @@ int elx_solve_resident(elx_ctx *ctx, int32_t solver, int32_t precision,
                        double tol, int32_t maxit, int32_t ngram,
                        elx_info *info);
 int elx_spmv_resident(elx_ctx *ctx, int32_t precision, int32_t reps);
+/* update_mec (Predict.f:183-209) on the resident state: u(j,i) =
+ * x(id(j,i)) for the free dofs, from the resident solution; with it a
+ * solvm pass (assemble, solve, update) and the stresses (elx_stress with
+ * u = NULL) never leave the device.  Stream-ordered like the calls above. */
+int elx_update_resident(elx_ctx *ctx);
 int elx_get_solution(elx_ctx *ctx, double *x);
 int elx_get_rhs(elx_ctx *ctx, double *b);
 

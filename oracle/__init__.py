@@ -72,6 +72,9 @@ def lib():
         L.orc_pform_edge_loads.argtypes = [I32P, I32P, F64P, I32P, I32P, F64P, F64P, C.c_int,
                                            C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]
         L.orc_pload.argtypes = [I32P, F64P, F64P, F64P, C.c_int, C.c_int]
+        L.orc_tform.argtypes = [I32P, I32P, F64P, C.c_int, F64P, F64P, C.c_void_p, C.c_int,
+                                C.c_int, C.c_int, C.c_int, C.c_int, F64P, I32P,
+                                C.POINTER(C.c_int)]
         L.orc_update.argtypes = [I32P, F64P, F64P, C.c_int, C.c_int]
         L.orc_matvec_csrcsym1.argtypes = [C.c_int, I32P, I32P, F64P, F64P, F64P, F64P]
         L.orc_dot.restype = C.c_double
@@ -181,6 +184,23 @@ def assemble(mesh, s: Structure, u=None, b0=None, lhs=True, rhs=True):
     if st:
         raise OracleError(st, f"element {bad.value}")
     return ad, al[:s.nad], b
+
+
+def tform(mesh, u, tx0=None):
+    """tform_mec (Pform.f:258-421) with the elements' isw = 3: nodal stresses
+    t (nnode, ntn), averaged over each node's elements, + tx0."""
+    L = lib()
+    ntn = 4 if mesh.ndm == 2 else 6
+    t = np.zeros((mesh.nnode, ntn))
+    ic = np.zeros(mesh.nnode, np.int32)
+    bad = C.c_int(0)
+    tx0p = None if tx0 is None else _f64(tx0).ctypes.data_as(C.c_void_p)
+    st = L.orc_tform(_i32(mesh.ix), _i32(mesh.ie), _f64(mesh.e), mesh.e.shape[1], _f64(mesh.x),
+                     _f64(u), tx0p, mesh.nnode, mesh.numel, mesh.nen, mesh.ndm, mesh.ndf, t, ic,
+                     C.byref(bad))
+    if st:
+        raise OracleError(st, f"element {bad.value}")
+    return t
 
 
 def colormsh(mesh):

@@ -827,6 +827,199 @@ int orc_pform_k(const int *ix, const int *ie, const double *e, int prop,
   return ORC_OK;
 }
 
+/* ---------------------------------------------------------------------- */
+/* Stress recovery: elmt02-07_mec isw = 3 and tform_mec (Pform.f:258-421)  */
+/* ---------------------------------------------------------------------- */
+
+/* Elmlib.f:2368-2411 deform2d */
+static void deform2d(const double *hx, const double *hy, const double *u, double *eps,
+                     int nen) {
+  double ux = 0.0, uy = 0.0, vx = 0.0, vy = 0.0;
+  for (int i = 0; i < nen; i++) {
+    ux = ux + hx[i] * u[2 * i];
+    uy = uy + hy[i] * u[2 * i];
+    vx = vx + hx[i] * u[2 * i + 1];
+    vy = vy + hy[i] * u[2 * i + 1];
+  }
+  eps[0] = ux;
+  eps[1] = vy;
+  eps[2] = uy + vx;
+}
+
+/* Elmlib.f:2413-2471 deform3d */
+static void deform3d(const double *hx, const double *hy, const double *hz, const double *u,
+                     double *eps, int nen) {
+  double ux = 0, uy = 0, uz = 0, vx = 0, vy = 0, vz = 0, wx = 0, wy = 0, wz = 0;
+  for (int i = 0; i < nen; i++) {
+    ux = ux + hx[i] * u[3 * i];
+    uy = uy + hy[i] * u[3 * i];
+    uz = uz + hz[i] * u[3 * i];
+    vx = vx + hx[i] * u[3 * i + 1];
+    vy = vy + hy[i] * u[3 * i + 1];
+    vz = vz + hz[i] * u[3 * i + 1];
+    wx = wx + hx[i] * u[3 * i + 2];
+    wy = wy + hy[i] * u[3 * i + 2];
+    wz = wz + hz[i] * u[3 * i + 2];
+  }
+  eps[0] = ux;
+  eps[1] = vy;
+  eps[2] = wz;
+  eps[3] = uy + vx;
+  eps[4] = vz + wy;
+  eps[5] = uz + wx;
+}
+
+/* Elmlib.f:2502-2538 stress2d_m: sxx, syy, szz (ps (sxx + syy) in plane
+ * strain, 0 in plane stress), sxy */
+static void stress2d_m(double d11, double d12, double d22, double d33, double ps, int ept,
+                       const double *eps, double *t) {
+  t[0] = d11 * eps[0] + d12 * eps[1];
+  t[1] = d12 * eps[0] + d22 * eps[1];
+  t[2] = ept ? ps * (t[0] + t[1]) : 0.0;
+  t[3] = d33 * eps[2];
+}
+
+/* Elmlib.f:2540-2571 stress3d */
+static void stress3d(double a, double b, double c, const double *eps, double *t) {
+  t[0] = (eps[0] + b * eps[1] + b * eps[2]) * a;
+  t[1] = (b * eps[0] + eps[1] + b * eps[2]) * a;
+  t[2] = (b * eps[0] + b * eps[1] + eps[2]) * a;
+  t[3] = eps[3] * c * a;
+  t[4] = eps[4] * c * a;
+  t[5] = eps[5] * c * a;
+}
+
+/* Constitutive constants of elmt02-07 (plane strain / 3-D: a, b, c of
+ * Elmlib02.f:179-186, 819-832, 1402-1408, 1697-1705; plane stress:
+ * Elmlib02.f:469-476, 1124-1134). */
+static void law(int plane_stress, double ym, double ps, double *a, double *b, double *c) {
+  if (!plane_stress) {
+    double a1 = 1.0 - ps, a2 = 1.0 - 2.0 * ps, a3 = 1.0 + ps;
+    *a = (ym * a1) / (a3 * a2);
+    *b = ps / a1;
+    *c = 0.5 * (a2 / a1);
+  } else {
+    double a1 = 1.0 - ps, a2 = 1.0 - ps * ps;
+    *a = ym / a2;
+    *b = ps;
+    *c = 0.5 * a1;
+  }
+}
+
+/* isw = 3 of elmt02-07_mec: stresses at the element's nodes, p(ntn, nen)
+ * col-major (ntn = 4 in 2-D, 6 in 3-D).  TRIA3 Elmlib02.f:235-250 (plane
+ * strain) / 525-540 (plane stress): constant, copied to the 3 nodes; QUAD4
+ * 836-846 / 1138-1148: at each node (rn, sn); TETRA4 1412-1437: constant;
+ * HEXA8 1798-1812: at each node (rn, sn, tn). */
+static int elmt_stress(int iel, const double *e, const double *x, int ndm, const double *u,
+                       double *p) {
+  static const double rn[8] = {1, -1, -1, 1, 1, -1, -1, 1};
+  static const double sn[8] = {1, 1, -1, -1, 1, 1, -1, -1};
+  static const double tn[8] = {1, 1, 1, 1, -1, -1, -1, -1};
+  const double ym = e[0], ps = e[1];
+  double a, b, c, eps[6];
+  switch (iel) {
+    case 2:
+    case 3: {
+      const int pstress = iel == 3;
+      law(pstress, ym, ps, &a, &b, &c);
+#define XX(q, n) x[(size_t)((n) - 1) * ndm + ((q) - 1)]
+      double xj11 = XX(1, 1) - XX(1, 3), xj12 = XX(2, 1) - XX(2, 3);
+      double xj21 = XX(1, 2) - XX(1, 3), xj22 = XX(2, 2) - XX(2, 3);
+#undef XX
+      double det = xj11 * xj22 - xj12 * xj21;
+      if (det <= 0.0) return ORC_ERR_BAD_DET;
+      double xji11 = xj22 / det, xji12 = -xj12 / det;
+      double xji21 = -xj21 / det, xji22 = xj11 / det;
+      double hx[3] = {xji11, xji12, -xji11 - xji12};
+      double hy[3] = {xji21, xji22, -xji21 - xji22};
+      deform2d(hx, hy, u, eps, 3);
+      stress2d_m(a, a * b, a, a * c, ps, !pstress, eps, p);
+      for (int n = 1; n < 3; n++)
+        for (int j = 0; j < 4; j++) p[4 * n + j] = p[j];
+      return ORC_OK;
+    }
+    case 4:
+    case 5: {
+      const int pstress = iel == 5;
+      law(pstress, ym, ps, &a, &b, &c);
+      for (int n = 0; n < 4; n++) {
+        double hx[4], hy[4], det;
+        sfquad4_m(hx, hy, rn[n], sn[n]);
+        if (jacob2d_m(hx, hy, x, 4, ndm, &det)) return ORC_ERR_BAD_DET;
+        deform2d(hx, hy, u, eps, 4);
+        stress2d_m(a, a * b, a, a * c, ps, !pstress, eps, p + 4 * n);
+      }
+      return ORC_OK;
+    }
+    case 6: {
+      law(0, ym, ps, &a, &b, &c);
+      double hx[4], hy[4], hz[4], det;
+      if (jtetra4(x, hx, hy, hz, &det)) return ORC_ERR_BAD_DET;
+      deform3d(hx, hy, hz, u, eps, 4);
+      stress3d(a, b, c, eps, p);
+      for (int n = 1; n < 4; n++)
+        for (int j = 0; j < 6; j++) p[6 * n + j] = p[j];
+      return ORC_OK;
+    }
+    case 7: {
+      law(0, ym, ps, &a, &b, &c);
+      for (int n = 0; n < 8; n++) {
+        double hx[8], hy[8], hz[8], det;
+        sfhexa8_m(hx, hy, hz, rn[n], sn[n], tn[n]);
+        if (jacob3d_m(hx, hy, hz, x, 8, &det)) return ORC_ERR_BAD_DET;
+        deform3d(hx, hy, hz, u, eps, 8);
+        stress3d(a, b, c, eps, p + 6 * n);
+      }
+      return ORC_OK;
+    }
+    default:
+      return ORC_ERR_BAD_ELEMENT;
+  }
+}
+
+/* Pform.f:258-421 tform_mec (isw = 3, every element node counted):
+ * t(ntn, nnode) = average over the elements of a node of their nodal
+ * stresses, + tx0 (may be NULL: zero).  ic(nnode) work array.  On a bad
+ * element returns its status and the element number in *bad_el. */
+int orc_tform(const int *ix, const int *ie, const double *e, int prop, const double *x,
+              const double *u, const double *tx0, int nnode, int numel, int nen, int ndm,
+              int ndf, double *t, int *ic, int *bad_el) {
+  const int nen1 = nen + 1, ntn = ndm == 2 ? 4 : 6;
+  double xl[3 * 8], ul[24], pl[6 * 8];
+  if (nen > 8 || ndf > 3 || ndm > 3) return ORC_ERR_ARG;
+  for (int i = 0; i < nnode; i++) {
+    ic[i] = 0;
+    for (int j = 0; j < ntn; j++) t[(size_t)i * ntn + j] = 0.0;
+  }
+  for (int nel = 1; nel <= numel; nel++) {
+    const int *ixe = &ix[(size_t)(nel - 1) * nen1];
+    int kk = 0;
+    for (int i = 0; i < nen; i++) {
+      const int no = ixe[i];
+      for (int j = 0; j < ndf; j++) ul[kk++] = u[(size_t)(no - 1) * ndf + j];
+    }
+    for (int i = 0; i < nen; i++)
+      for (int j = 0; j < ndm; j++) xl[i * ndm + j] = x[(size_t)(ixe[i] - 1) * ndm + j];
+    const int ma = ixe[nen];
+    int st = elmt_stress(ie[ma - 1], &e[(size_t)(ma - 1) * prop], xl, ndm, ul, pl);
+    if (st) {
+      if (bad_el) *bad_el = nel;
+      return st;
+    }
+    for (int i = 0; i < nen; i++) {
+      const int no = ixe[i];
+      if (no <= 0) continue;
+      ic[no - 1] += 1;
+      for (int j = 0; j < ntn; j++) t[(size_t)(no - 1) * ntn + j] += pl[i * ntn + j];
+    }
+  }
+  for (int i = 0; i < nnode; i++)
+    for (int j = 0; j < ntn; j++)
+      t[(size_t)i * ntn + j] = t[(size_t)i * ntn + j] / ic[i] + (tx0 ? tx0[(size_t)i * ntn + j] : 0.0);
+  return ORC_OK;
+}
+
 /* Colormsh.f:9-308 coloredmesh with omp_elmt = .true.: nodegrade +
  * elmincid + colormsh (greedy, at most 200 colours) + setcolor.
  * elcolor (numel) receives the elements colour by colour (1-based),
