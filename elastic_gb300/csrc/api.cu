@@ -110,7 +110,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
   for (DBuf *v : {&c->iat, &c->jat, &c->pt, &c->ja16, &c->jat16, &c->tile_tgt, &c->tile_out,
                   &c->tgt_col, &c->tgt_start, &c->tpos, &c->halo_ptr, &c->halo_slot,
                   &c->tile_desc, &c->part, &c->alt, &c->bia, &c->bja, &c->bt, &c->bval,
-                  &c->bval32})
+                  &c->bval32, &c->sell_ptr, &c->sell_col, &c->sell_val})
     c->release(*v);
   if (c->use_blocks) {
     // the node-block product replaces both scalar kernel families
@@ -152,7 +152,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
   release_block(c);
   c->tuned_width[0] = c->tuned_width[1] = 0;
   for (DBuf *v : {&c->node_count, &c->tstress, &c->tx0buf}) c->release(*v);
-  c->have_fp32 = false;
+  c->have_fp32 = 0;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
   c->alloc(c->b0, n * 8);
@@ -174,13 +174,16 @@ void upload_structure(elx_ctx *c, bool prederived) {
 }
 
 // FP32 copies of the matrix (after each assembly) and the FP32 inner-solver
-// vectors (once per structure), allocated on first use.
-void ensure_fp32(elx_ctx *c) {
+// vectors (once per structure), allocated on first use.  With node blocks the
+// single-vector product reads the sliced copy and the block solver the
+// block-major one (`block`); each is made only when its solver asks.
+void ensure_fp32(elx_ctx *c, bool block = false) {
   const size_t n = (size_t)c->s.neq, nad = (size_t)c->s.nad;
+  // the lane-group product (group_lanes > 0) reads the block-major copy too
+  block = block || c->group_lanes > 0;
+  const int want = block ? kFp32Block : kFp32Single;
   if (!c->m32.p) {
-    if (c->use_blocks) {
-      c->alloc(c->bval32, (size_t)c->s.nnzb * c->s.bsize * c->s.bsize * 4 + 64);
-    } else {
+    if (!c->use_blocks) {
       c->alloc(c->ad32, n * 4 + 64);
       c->alloc(c->al32, nad * 4 + 64);
       c->alloc(c->alt32, nad * 4 + 64);
@@ -188,15 +191,35 @@ void ensure_fp32(elx_ctx *c) {
     for (DBuf *v : {&c->m32, &c->p32, &c->q32, &c->r32, &c->x32}) c->alloc(*v, n * 4 + 64);
     c->drop_graphs();
   }
-  if (c->have_fp32) return;
-  if (c->use_blocks) {
-    elx::launch_demote_blocks(c->csrc_dev(), c->stream);
-    c->launches += 1;
-  } else {
+  if (c->use_blocks && block && !c->bval32.p) {
+    c->alloc(c->bval32, (size_t)c->s.nnzb * c->s.bsize * c->s.bsize * 4 + 64);
+    c->drop_graphs();
+  }
+  if (c->use_blocks && !block && !c->sell_val.p) {
+    c->upload(c->sell_ptr, c->s.sell_ptr.data(), c->s.sell_ptr.size());
+    c->upload(c->sell_col, c->s.sell_col.data(), c->s.sell_col.size());
+    const size_t bytes =
+        (size_t)c->s.sell_ptr[c->s.nslices] * elx::kSliceRows * c->s.bsize * c->s.bsize * 4;
+    c->alloc(c->sell_val, bytes + 64);
+    int l2 = 0;
+    ELX_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device));
+    c->sell_stream = (double)(bytes + c->sell_col.bytes) > 0.6 * l2;
+    if (const char *env = getenv("ELX_SELL_STREAM")) c->sell_stream = atoi(env) != 0;
+    c->drop_graphs();
+  }
+  if (c->have_fp32 & want) return;
+  if (!c->use_blocks) {
     elx::launch_demote_values(c->csrc_dev(), c->stream);
     c->launches += c->s.nad ? 2 : 1;
+    c->have_fp32 |= kFp32Single | kFp32Block;
+  } else {
+    if (block)
+      elx::launch_demote_blocks(c->csrc_dev(), c->stream);
+    else
+      elx::launch_demote_sell(c->csrc_dev(), c->stream);
+    c->launches += 1;
+    c->have_fp32 |= want;
   }
-  c->have_fp32 = true;
 }
 
 // The kernel-side copies of a new CSRC matrix: the node blocks, or the
@@ -230,7 +253,7 @@ void assemble_resident(elx_ctx *c) {
   c->launches += (int64_t)s.segments.size();
   ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   c->sync();
-  c->have_fp32 = false;
+  c->have_fp32 = 0;
   if (c->h_flags[0] != INT_MAX) {
     c->have_matrix = false;
     throw Error{ELX_ERR_BAD_DET, "non-positive Jacobian determinant in element " +
@@ -652,7 +675,7 @@ int autotune_block_width(elx_ctx *c, bool mixed, double *times_us = nullptr) {
   const int slot = mixed ? 1 : 0;
   if (c->tuned_width[slot] && !times_us) return c->tuned_width[slot];
   ensure_block(c, kMaxBlockWidth, mixed);
-  if (mixed) ensure_fp32(c);
+  if (mixed) ensure_fp32(c, true);
   const size_t n = (size_t)c->s.neq;
   ELX_CUDA(cudaMemsetAsync(c->bk_p.p, 0, n * kMaxBlockWidth * 8, c->stream));
   if (mixed) ELX_CUDA(cudaMemsetAsync(c->bk_p32.p, 0, n * kMaxBlockWidth * 4, c->stream));
@@ -702,7 +725,7 @@ void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int
           "block solves need node blocks (every node all free or all fixed)");
   const bool mixed = precision == ELX_PREC_MIXED;
   auto t0 = std::chrono::steady_clock::now();
-  if (mixed) ensure_fp32(c);
+  if (mixed) ensure_fp32(c, true);
   build_preconditioner(c);
   if (width == 0) width = autotune_block_width(c, mixed);
   int w = 1;
@@ -967,7 +990,8 @@ void elx_destroy(elx_ctx *c) {
                   &c->halo_ptr, &c->halo_slot, &c->tile_desc, &c->part, &c->ad, &c->al,
                   &c->ad32, &c->al32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32,
                   &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate,
-                  &c->bia, &c->bja, &c->bt, &c->bval, &c->bval32,
+                  &c->bia, &c->bja, &c->bt, &c->bval, &c->bval32, &c->sell_ptr, &c->sell_col,
+                  &c->sell_val,
                   &c->node_count, &c->tstress, &c->tx0buf,
                   &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
                   &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
@@ -1165,7 +1189,7 @@ int elx_set_matrix(elx_ctx *c, const double *ad, const double *al) {
     refresh_derived_values(c);
     c->sync();
     c->have_matrix = true;
-    c->have_fp32 = false;
+    c->have_fp32 = 0;
   });
 }
 

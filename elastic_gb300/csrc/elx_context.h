@@ -11,6 +11,8 @@
 using elx::DBuf;
 using elx::Error;
 
+constexpr int kFp32Single = 1, kFp32Block = 2;
+
 struct elx_ctx {
   int device = 0;
   int verbose = 0;
@@ -21,13 +23,22 @@ struct elx_ctx {
   elx::Mesh mesh;
   elx::Structure s;
   bool have_mesh = false, have_structure = false, have_matrix = false;
-  bool have_fp32 = false;
+  // FP32 matrix copies made since the last assembly: kFp32Single (the
+  // single-vector product's: sliced node blocks, or the scalar CSRC arrays),
+  // kFp32Block (block-major node blocks, for the block solver)
+  int have_fp32 = 0;
 
   // mesh (colour order) and structure
   DBuf conn, mat, elnum, slot, x, eq, e;
   DBuf ia, ja, iat, jat, pt, ja16, jat16;
   // node blocks (when the numbering allows them): pattern and values
   DBuf bia, bja, bt, bval, bval32;
+  // the FP32 sliced copy of the node blocks and its pattern; read with
+  // streaming loads unless it fits in 60 % of L2 (ELX_SELL_STREAM=0/1 forces
+  // either: 49.7 against 54.5 us on the 64^3 HEXA8 cube, 277 MB; 17.2
+  // against 12.6 us on the 48^3 TETRA4 mesh, 64 MB)
+  DBuf sell_ptr, sell_col, sell_val;
+  bool sell_stream = true;
   bool use_blocks = false;
   // tiled transposed index of the SpMV and its halo slots
   DBuf tile_tgt, tile_out, tgt_col, tgt_start, tpos, halo_ptr, halo_slot, tile_desc, part;
@@ -36,11 +47,12 @@ struct elx_ctx {
   int spmv_kind = elx::kSpmvGather;  // FP64 SpMV kernel family
   bool use_delta = true;             // 16-bit column deltas when the bandwidth fits
   int gather_blocks = 0;             // gather SpMV grid (0: default)
-  // FP32 node-block product: lanes per block row (16 and 8 measured alike,
+  // FP32 node-block product: 0 = the sliced kernel, else the lane-group
+  // kernel with this many lanes per block row (16 and 8 measured alike,
   // 68.8 / 67.9 us on the 64^3 HEXA8 cube and 20.8 us on the 48^3 TETRA4
   // mesh, against 86.3 / 24.5 us for one thread per row and 80.4 / 31.0 us
   // for 32 lanes)
-  int group_lanes = 16;
+  int group_lanes = 0;
   // state and solver vectors
   DBuf u, b0, b, xs, r, p, q, m, z;
   // mixed precision: FP32 inner PCG vectors and preconditioner
@@ -141,6 +153,10 @@ struct elx_ctx {
       k.bia = bia.as<int32_t>(); k.bja = bja.as<int32_t>(); k.bt = bt.as<int32_t>();
       k.bval = bval.as<double>(); k.bval32 = bval32.as<float>();
       k.group_lanes = group_lanes;
+      k.nslices = s.nslices;
+      k.sell_ptr = sell_ptr.as<int32_t>(); k.sell_col = sell_col.as<int32_t>();
+      k.sell_val = sell_val.as<float>();
+      k.sell_stream = sell_stream;
     }
     return k;
   }

@@ -113,7 +113,16 @@ struct Structure {
   int32_t bsize = 0, nb = 0;
   int64_t nnzb = 0;
   std::vector<int32_t> bia, bja, bt;
+  // Sliced copy of the node blocks for the FP32 product: block rows in
+  // slices of kSliceRows; slice s is sell_ptr[s + 1] - sell_ptr[s] slot
+  // groups wide (its longest row), and slot (g, t) is block g - sell_ptr[s]
+  // of block row kSliceRows s + t, with block column sell_col[kSliceRows g + t]
+  // (padding slots: the row's own column, zero values).
+  int32_t nslices = 0;
+  std::vector<int32_t> sell_ptr, sell_col;
 };
+
+constexpr int kSliceRows = 32;
 
 // host structure routines (structure.cpp)
 void node_graph(const Mesh &m, std::vector<int32_t> &xadj, std::vector<int32_t> &adj);
@@ -160,7 +169,13 @@ struct CsrcDev {
   const int32_t *bia = nullptr, *bja = nullptr, *bt = nullptr;
   double *bval = nullptr;
   float *bval32 = nullptr;
-  int32_t group_lanes = 16;  // FP32 node-block product: lanes per block row (16 or 32)
+  // FP32 node-block product: 0 = the sliced kernel (sell_*), else the
+  // lane-group kernel with this many lanes per block row (reads bval32)
+  int32_t group_lanes = 0;
+  int32_t nslices = 0;
+  const int32_t *sell_ptr = nullptr, *sell_col = nullptr;
+  float *sell_val = nullptr;
+  bool sell_stream = true;  // streaming loads (the copy does not stay in L2)
 };
 
 struct TileDev {
@@ -196,6 +211,8 @@ void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
 // Node-block values from the CSRC arrays (k.bval), and their FP32 copy.
 void launch_fill_blocks(const CsrcDev &k, cudaStream_t st);
 void launch_demote_blocks(const CsrcDev &k, cudaStream_t st);
+// FP32 sliced copy of k.bval (k.sell_val)
+void launch_demote_sell(const CsrcDev &k, cudaStream_t st);
 // Two-sided gather SpMV: y = K x reading the lower part (ja, al) and the
 // upper part through the transposed copy (jat, alt); with sc != nullptr it
 // also forms (x, y) and alpha = d / (x, y).

@@ -1,6 +1,6 @@
 // Thin inline-PTX wrappers for the asynchronous copy machinery of sm_100+:
 // mbarriers, 1-D bulk copies (cp.async.bulk, the TMA engine's non-tensor
-// form) and per-thread cp.async gathers.  Every wait is bounded: a wait that
+// form), per-thread cp.async gathers and streaming loads.  Every wait is bounded: a wait that
 // gives up records an error code in a device word instead of spinning
 // forever, and the host turns it into ELX_ERR_TIMEOUT.
 #pragma once
@@ -91,6 +91,29 @@ __device__ __forceinline__ void cp_async_wait() {
 
 __device__ __forceinline__ void named_barrier(int id, int threads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// Streaming loads of read-only data that is used once (matrix values and
+// indices): not kept in L1, and issued in program order (volatile), so that a
+// group of them is in flight before the first use.
+__device__ __forceinline__ float4 ld_stream4(const float *p) {
+  float4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ float ld_stream(const float *p) {
+  float v;
+  asm volatile("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ int32_t ld_stream(const int32_t *p) {
+  int32_t v;
+  asm volatile("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
 }
 
 }  // namespace ptx

@@ -536,6 +536,9 @@ void build_blocks(Structure &s, int bsize) {
   s.bia.clear();
   s.bja.clear();
   s.bt.clear();
+  s.nslices = 0;
+  s.sell_ptr.clear();
+  s.sell_col.clear();
   const int B = bsize;
   if (B < 2 || B > 3 || s.neq % B) return;
   const int nb = s.neq / B;
@@ -589,6 +592,25 @@ void build_blocks(Structure &s, int bsize) {
   s.bsize = B;
   s.nb = nb;
   s.nnzb = nnzb;
+  // the sliced copy's pattern: each slice as wide as its longest block row
+  const int R = kSliceRows;
+  s.nslices = (nb + R - 1) / R;
+  s.sell_ptr.assign(s.nslices + 1, 0);
+  for (int sl = 0; sl < s.nslices; sl++) {
+    int w = 0;
+    for (int I = sl * R; I < std::min(nb, sl * R + R); I++) w = std::max(w, s.bia[I + 1] - s.bia[I]);
+    s.sell_ptr[sl + 1] = s.sell_ptr[sl] + w;
+  }
+  s.sell_col.assign((size_t)s.sell_ptr[s.nslices] * R, 0);
+  for (int sl = 0; sl < s.nslices; sl++)
+    for (int t = 0; t < R; t++) {
+      const int I = sl * R + t;
+      const int n = I < nb ? s.bia[I + 1] - s.bia[I] : 0;
+      for (int g = s.sell_ptr[sl]; g < s.sell_ptr[sl + 1]; g++) {
+        const int k = g - s.sell_ptr[sl];
+        s.sell_col[(size_t)g * R + t] = k < n ? s.bja[s.bia[I] + k] : (I < nb ? I : 0);
+      }
+    }
 }
 
 }  // namespace elx

@@ -251,6 +251,25 @@ def test_fp32_spmv_parity(gpu_ctx, name):
     assert rel_inf(y_o, y_g) <= FP32_SPMV_TOL
 
 
+@pytest.mark.parametrize("env", [{"ELX_GROUP_LANES": "16"}, {"ELX_SELL_STREAM": "0"},
+                                 {"ELX_SELL_STREAM": "1"}])
+@pytest.mark.parametrize("name", ["quad4_stress", "hexa8"])
+def test_fp32_spmv_kernel_choices(built_lib, monkeypatch, name, env):
+    """Each FP32 node-block product (sliced copy with streaming or cached
+    loads; lane groups on the block-major copy) against the FP64 oracle."""
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    m = MESHES[name]()
+    ctx = E.Context(device=0)
+    try:
+        s = _setup(ctx, m)
+        _, ad, al = ctx.assemble(None, None, want_matrix=True)
+        x = np.random.default_rng(5).standard_normal(s.neq)
+        assert rel_inf(O.matvec(s, ad, al, x), ctx.spmv(x, precision=E.PREC_MIXED)) <= FP32_SPMV_TOL
+    finally:
+        ctx.close()
+
+
 @pytest.mark.parametrize("name", ["quad4_stress", "tetra4", "hexa8"])
 def test_mixed_precision_refinement_matches_fp64(gpu_ctx, name):
     """FP32 inner PCG + FP64 refinement meets the reference's FP64 stopping
