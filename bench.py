@@ -142,7 +142,7 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def profiled(key, name="bcsr_spmv_fp64_hexa8_cube64.md"):
+def profiled(key, name="sell_spmv_fp64_hexa8_cube64.md"):
     """A figure (`key: value` line) from a committed ncu summary, if any."""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
@@ -279,7 +279,7 @@ def run_ours(args, dist: Dist):
             "pcg_ms": pcg_ms, "pcg_iter_gbs": iter_gbs, "spmv_ms": spmv_ms,
             "spmv_gbs": spmv_gbs, "wall_s": wall,
             "roofline": {"bound": "hbm",
-                         "kernel": "bcsr_spmv_kernel<double> (FP64 node-block SpMV + fused (p, Kp))",
+                         "kernel": "sell_spmv_kernel<double> (FP64 sliced node-block SpMV + fused (p, Kp))",
                          "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
                          "frac": spmv_gbs / peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": spmv_bytes,

