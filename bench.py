@@ -9,7 +9,11 @@ One step = one pass of the hot path: element integration + CSRC assembly
 (pform_mec isw=2) and the PCG solve to tolerance (solv).  `value` is solves/s
 with the mesh, structure and load vectors already resident on the device;
 `e2e` is the same through the C ABI with host buffers (u, b0 in, b out;
-b in, x out) copied every step.
+b in, x out) copied every step.  Sub-objects: `mixed` (the same step with
+the mixed-precision solver), `after_solve` (the device load step and stress
+recovery on the solution, against the oracle's stress recovery), `block`
+(16 load cases of the 96x96x48 plate) and `serve` (a served request stream
+against sequential plain FP64 solves).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -263,6 +267,31 @@ def run_ours(args, dist: Dist):
     h2d = (u0.size + 2 * neq) * 8
     d2h = 2 * neq * 8
 
+    # ---- the rows after the solve: the load step on the device (pload_mec:
+    # f up, b0 and u formed there) and stress recovery (tform_mec with the
+    # elements' isw = 3, nodal stresses back to the host), each through its
+    # C ABI call on the resident solution
+    f_h = pin(mesh.f)
+    ctx.set_state(None, None)
+    ctx.set_loads(f_h)
+    ctx.assemble_resident()
+    ctx.solve_resident(tol=TOL, maxit=MAXIT)
+    ctx.update_resident()
+    ld_s, sr_s = [], []
+    for k in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        ctx.set_loads(f_h)
+        t1 = time.perf_counter()
+        stresses = ctx.stress(None)
+        t2 = time.perf_counter()
+        if k >= args.warmup:
+            ld_s.append(t1 - t)
+            sr_s.append(t2 - t1)
+    u_sol, _ = ctx.state()
+    nxt = {"loads_ms": 1e3 * statistics.median(ld_s), "loads_h2d_bytes": mesh.f.size * 8,
+           "stress_ms": 1e3 * statistics.median(sr_s),
+           "stress_d2h_bytes": stresses.size * 8, "elements": mesh.numel}
+
     out = None
     if dist.rank == 0:
         n = dist.ws
@@ -302,6 +331,16 @@ def run_ours(args, dist: Dist):
         }
         if n == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(mesh, st, b0, u0, iters, sample_iters=300)
+            # the oracle's stress recovery (one host thread) on the same u,
+            # and how far the device's nodal stresses are from it
+            import oracle as O
+            t = time.perf_counter()
+            t_o = O.tform(mesh, u_sol)
+            nxt["stress_cpu_oracle_ms"] = 1e3 * (time.perf_counter() - t)
+            nxt["stress_cpu_cores"] = 1
+            nxt["stress_max_rel_diff_vs_oracle"] = float(
+                np.abs(t_o - stresses).max() / np.abs(t_o).max())
+        out["after_solve"] = nxt
     ctx.close()
     return out
 

@@ -138,6 +138,8 @@ def load():
         "elx_autotune_block": (C.c_int, [_VP, C.c_int32, P(C.c_int32), _VP]),
         "elx_stress": (C.c_int, [_VP, _VP, _VP, _VP]),
         "elx_update_resident": (C.c_int, [_VP]),
+        "elx_set_loads": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32]),
+        "elx_get_state": (C.c_int, [_VP, _VP, _VP]),
         "elx_server_create": (C.c_int, [P(_VP), P(ServerOpts)]),
         "elx_server_destroy": (None, [_VP]),
         "elx_server_submit": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
@@ -387,6 +389,25 @@ class Context:
     def set_state(self, u=None, b0=None):
         self._check(self._L.elx_set_state(self._h, _ptr(None if u is None else _f64(u)),
                                           _ptr(None if b0 is None else _f64(b0))))
+
+    def set_loads(self, f, eload=None, loadvec=None):
+        """pload_mec + the 2-D edge loads (isw = 4) on the device, into the
+        resident b0 and u: f (nnode, ndf) evaluated nodal loads, eload
+        (numel, 7) 1-based load numbers per side, loadvec (nload, 2)."""
+        ff = _f64(f)
+        el = None if eload is None else np.ascontiguousarray(eload, dtype=np.int32)
+        lv = None if loadvec is None else _f64(np.asarray(loadvec, np.float64).reshape(-1, 2))
+        nload = 0 if lv is None else lv.shape[0]
+        self._check(self._L.elx_set_loads(self._h, _ptr(ff), _ptr(el), _ptr(lv), nload))
+
+    def state(self):
+        """The resident (u (nnode, ndf), b0 (neq,))."""
+        m = self.mesh
+        neq, _, _ = self.sizes()
+        u = np.zeros((m.nnode, m.ndf))
+        b0 = np.zeros(neq)
+        self._check(self._L.elx_get_state(self._h, _ptr(u), _ptr(b0)))
+        return u, b0
 
     def assemble_resident(self):
         self._check(self._L.elx_assemble_resident(self._h))

@@ -152,7 +152,9 @@ void upload_structure(elx_ctx *c, bool prederived) {
     c->release(*v);
   release_block(c);
   c->tuned_width[0] = c->tuned_width[1] = 0;
-  for (DBuf *v : {&c->node_count, &c->tstress, &c->tx0buf}) c->release(*v);
+  for (DBuf *v : {&c->node_count, &c->tstress, &c->tx0buf, &c->fbuf, &c->ld_node, &c->ld_ptr,
+                  &c->ld_ent, &c->ld_vec})
+    c->release(*v);
   c->have_fp32 = 0;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
@@ -1021,7 +1023,8 @@ void elx_destroy(elx_ctx *c) {
                   &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate,
                   &c->bia, &c->bja, &c->bt, &c->bval, &c->bval32, &c->sell_ptr, &c->sell_col,
                   &c->sell_val, &c->sell_val64,
-                  &c->node_count, &c->tstress, &c->tx0buf,
+                  &c->node_count, &c->tstress, &c->tx0buf, &c->fbuf, &c->ld_node, &c->ld_ptr,
+                  &c->ld_ent, &c->ld_vec,
                   &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
                   &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
     c->release(*d);
@@ -1175,6 +1178,63 @@ int elx_set_state(elx_ctx *c, const double *u, const double *b0) {
                                c->stream));
     else
       ELX_CUDA(cudaMemsetAsync(c->b0.p, 0, c->b0.bytes, c->stream));
+    c->sync();
+  });
+}
+
+int elx_set_loads(elx_ctx *c, const double *f, const int32_t *eload, const double *loadvec,
+                  int32_t nload) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "set the structure first");
+    require(f != nullptr, ELX_ERR_ARG, "null f");
+    const elx::Mesh &m = c->mesh;
+    const size_t nf = (size_t)m.ndf * m.nnode;
+    std::vector<int32_t> node, ptr, ent;
+    if (eload) {
+      require(m.ndm == 2 && m.ndf == 2, ELX_ERR_ARG,
+              "distributed edge loads are 2-D only (the reference stops on 3-D element loads)");
+      require(nload >= 0 && (nload == 0 || loadvec), ELX_ERR_ARG, "null loadvec");
+      int32_t bad_el = 0;
+      if (!elx::build_edge_lists(m, eload, nload, node, ptr, ent, bad_el))
+        throw Error{ELX_ERR_ARG, "bad load number or unloadable side in element " +
+                                     std::to_string(bad_el)};
+    }
+    if (!c->fbuf.p) c->alloc(c->fbuf, nf * 8);
+    ELX_CUDA(cudaMemcpyAsync(c->fbuf.p, f, nf * 8, cudaMemcpyHostToDevice, c->stream));
+    elx::launch_pload((int64_t)nf, c->eq.as<int32_t>(), c->fbuf.as<double>(), c->u.as<double>(),
+                      c->b0.as<double>(), c->stream);
+    c->launches += 1;
+    if (!node.empty()) {
+      c->upload(c->ld_node, node.data(), node.size());
+      c->upload(c->ld_ptr, ptr.data(), ptr.size());
+      c->upload(c->ld_ent, ent.data(), ent.size());
+      c->upload(c->ld_vec, loadvec, (size_t)nload * 2);
+      const int32_t big = INT_MAX;
+      int32_t *bad = c->flags.as<int32_t>();
+      ELX_CUDA(cudaMemcpyAsync(bad, &big, sizeof(big), cudaMemcpyHostToDevice, c->stream));
+      elx::launch_edge_loads((int)node.size(), c->ld_node.as<int32_t>(), c->ld_ptr.as<int32_t>(),
+                             c->ld_ent.as<int32_t>(), c->x.as<double>(), c->eq.as<int32_t>(),
+                             c->ld_vec.as<double>(), c->b0.as<double>(), bad, c->stream);
+      c->launches += 1;
+      ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                               c->stream));
+    }
+    c->sync();
+    if (!node.empty() && c->h_flags[0] != INT_MAX)
+      throw Error{ELX_ERR_BAD_DET, "zero-length loaded side in element " +
+                                       std::to_string(c->h_flags[0])};
+  });
+}
+
+int elx_get_state(elx_ctx *c, double *u, double *b0) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "set the structure first");
+    if (u)
+      ELX_CUDA(cudaMemcpyAsync(u, c->u.p, (size_t)c->mesh.ndf * c->mesh.nnode * 8,
+                               cudaMemcpyDeviceToHost, c->stream));
+    if (b0)
+      ELX_CUDA(cudaMemcpyAsync(b0, c->b0.p, (size_t)c->s.neq * 8, cudaMemcpyDeviceToHost,
+                               c->stream));
     c->sync();
   });
 }

@@ -59,6 +59,8 @@ struct elx_ctx {
   DBuf m32, p32, q32, r32, x32;
   // stress recovery: elements per node, nodal stresses, initial stresses
   DBuf node_count, tstress, tx0buf;
+  // device loads: nodal loads f, edge-load lists and load vectors
+  DBuf fbuf, ld_node, ld_ptr, ld_ent, ld_vec;
   // BiCGSTAB (r0, t) and GMRES (Krylov basis, small dense arrays, state)
   DBuf r0v, tv, gbasis, garrays, gstate;
   // block PCG: multi-vectors of up to blk_cap columns, scalars, staging

@@ -207,6 +207,17 @@ void launch_stress(const MeshDev &m, const Segment &seg, const double *u, double
 void launch_stress_average(int nnode, int ntn, const int32_t *count, const double *tx0,
                            double *ts, cudaStream_t st);
 void launch_update(int64_t n, const int32_t *eq, const double *x, double *u, cudaStream_t st);
+// Loads (loads.cu): pload_mec into the resident b0/u, then the 2-D edge
+// loads of pform_mec isw = 4 from host-built integer lists.
+constexpr int kEdgeEntryInts = 8;
+bool build_edge_lists(const Mesh &m, const int32_t *eload, int32_t nload,
+                      std::vector<int32_t> &node, std::vector<int32_t> &ptr,
+                      std::vector<int32_t> &ent, int32_t &bad_el);
+void launch_pload(int64_t n, const int32_t *eq, const double *f, double *u, double *b0,
+                  cudaStream_t st);
+void launch_edge_loads(int nnodes, const int32_t *node, const int32_t *ptr, const int32_t *ent,
+                       const double *x, const int32_t *eq, const double *loadvec, double *b0,
+                       int32_t *bad, cudaStream_t st);
 void launch_demote_values(const CsrcDev &k, cudaStream_t st);
 void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
 // Node-block values from the CSRC arrays (k.bval), and their FP32 copy.

@@ -261,6 +261,21 @@ int elx_set_matrix(elx_ctx *ctx, const double *ad, const double *al);
  * elx_stream(ctx) and return once enqueued, except elx_solve_resident which
  * waits for convergence. */
 int elx_set_state(elx_ctx *ctx, const double *u, const double *b0);
+/* The load step on the device (replaces the host's pload_mec, Pload.f:2-58,
+ * and pform_mec with isw = 4, Pform.f:1-11 / Elmlib02.f:260-314, 856-910):
+ * f(ndf,nnode) evaluated nodal loads -> b0(id) = f for free dofs, u = f for
+ * prescribed ones (free dofs of u keep their value); then, if eload is not
+ * NULL, the 2-D distributed edge loads: eload(7,numel) 1-based load numbers
+ * per element side (0: unloaded), loadvec(2,nload) the loads' traction
+ * vectors (type 40); b0(k) -= the element vectors, bitwise as the reference
+ * forms them.  The results stay resident for elx_assemble_resident.
+ * ELX_ERR_ARG for a load number outside 1..nload, a loaded side an element
+ * does not have, or edge loads on a 3-D mesh; ELX_ERR_BAD_DET for a
+ * zero-length loaded side. */
+int elx_set_loads(elx_ctx *ctx, const double *f, const int32_t *eload,
+                  const double *loadvec, int32_t nload);
+/* Copy the resident u(ndf,nnode) and b0(neq) to the host (either NULL). */
+int elx_get_state(elx_ctx *ctx, double *u, double *b0);
 int elx_assemble_resident(elx_ctx *ctx);
 int elx_solve_resident(elx_ctx *ctx, int32_t solver, int32_t precision,
                        double tol, int32_t maxit, int32_t ngram,
