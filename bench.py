@@ -10,8 +10,9 @@ One step = one pass of the hot path: element integration + CSRC assembly
 with the mesh, structure and load vectors already resident on the device;
 `e2e` is the same through the C ABI with host buffers (u, b0 in, b out;
 b in, x out) copied every step.  Sub-objects: `mixed` (the same step with
-the mixed-precision solver), `after_solve` (the device load step and stress
-recovery on the solution, against the oracle's stress recovery), `block`
+the mixed-precision solver), `after_solve` (the device load step, stress
+recovery and the result file on the solution, against the oracle's stress
+recovery and writer), `block`
 (16 load cases of the 96x96x48 plate) and `serve` (a served request stream
 against sequential plain FP64 solves).
 
@@ -288,9 +289,21 @@ def run_ours(args, dist: Dist):
             ld_s.append(t1 - t)
             sr_s.append(t2 - t1)
     u_sol, _ = ctx.state()
+    # the result file (write_mesh_res_mec, XML VTU ASCII with u and stresses)
+    # formatted on the device, copied back and written to a scratch file
+    import tempfile
+    vtk_dir = tempfile.mkdtemp(prefix="elx_vtk_")
+    vtk_path = os.path.join(vtk_dir, "res.vtu")
+    vt_s = []
+    for k in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        vtk_bytes = ctx.write_vtk(vtk_path)
+        if k >= args.warmup:
+            vt_s.append(time.perf_counter() - t)
     nxt = {"loads_ms": 1e3 * statistics.median(ld_s), "loads_h2d_bytes": mesh.f.size * 8,
            "stress_ms": 1e3 * statistics.median(sr_s),
-           "stress_d2h_bytes": stresses.size * 8, "elements": mesh.numel}
+           "stress_d2h_bytes": stresses.size * 8, "elements": mesh.numel,
+           "vtk_ms": 1e3 * statistics.median(vt_s), "vtk_bytes": vtk_bytes}
 
     out = None
     if dist.rank == 0:
@@ -340,7 +353,16 @@ def run_ours(args, dist: Dist):
             nxt["stress_cpu_cores"] = 1
             nxt["stress_max_rel_diff_vs_oracle"] = float(
                 np.abs(t_o - stresses).max() / np.abs(t_o).max())
+            # the oracle's writer (one host thread) on the same u and stresses
+            ref_path = os.path.join(vtk_dir, "ref.vtu")
+            t = time.perf_counter()
+            O.write_mesh_res(ref_path, mesh, u_sol, stresses, 0)
+            nxt["vtk_cpu_oracle_ms"] = 1e3 * (time.perf_counter() - t)
+            with open(vtk_path, "rb") as a, open(ref_path, "rb") as b:
+                nxt["vtk_identical_to_oracle"] = a.read() == b.read()
         out["after_solve"] = nxt
+    import shutil
+    shutil.rmtree(vtk_dir, ignore_errors=True)
     ctx.close()
     return out
 

@@ -33,6 +33,8 @@ OK, ERR_ZERO_DIAG, ERR_NO_CONVERGENCE, ERR_BAD_DET, ERR_OOM, ERR_TIMEOUT, ERR_AR
     ERR_BAD_ELEMENT, ERR_CUDA, ERR_STATE = range(10)
 SOLVER_PCG, SOLVER_GMRES, SOLVER_BICGSTAB = 1, 2, 4
 PREC_FP64, PREC_MIXED = 0, 1
+VTK_VTU_ASCII, VTK_LEGACY_BINARY = 0, 1   # result file formats
+VTK_DESLOC, VTK_STRESS = 1, 2             # result fields (fprint(2), fprint(3))
 
 STATUS_NAMES = {0: "ok", 1: "zero diagonal", 2: "no convergence", 3: "bad determinant",
                 4: "out of memory", 5: "timeout", 6: "bad argument",
@@ -139,6 +141,9 @@ def load():
         "elx_stress": (C.c_int, [_VP, _VP, _VP, _VP]),
         "elx_update_resident": (C.c_int, [_VP]),
         "elx_set_loads": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32]),
+        "elx_write_vtk": (C.c_int, [_VP, C.c_char_p, C.c_int32, C.c_int32, _VP]),
+        "elx_format_vtk": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP, C.c_int64, _VP]),
+        "elx_fortran_e": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _VP]),
         "elx_get_state": (C.c_int, [_VP, _VP, _VP]),
         "elx_server_create": (C.c_int, [P(_VP), P(ServerOpts)]),
         "elx_server_destroy": (None, [_VP]),
@@ -400,6 +405,21 @@ class Context:
         nload = 0 if lv is None else lv.shape[0]
         self._check(self._L.elx_set_loads(self._h, _ptr(ff), _ptr(el), _ptr(lv), nload))
 
+    def format_vtk(self, fmt=VTK_VTU_ASCII, fields=VTK_DESLOC | VTK_STRESS) -> bytes:
+        """write_mesh_res_mec's file, formatted on the GPU, as bytes."""
+        n = C.c_int64(0)
+        self._check(self._L.elx_format_vtk(self._h, fmt, fields, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(max(n.value, 1))
+        self._check(self._L.elx_format_vtk(self._h, fmt, fields, C.cast(buf, _VP), n.value,
+                                           C.byref(n)))
+        return buf.raw[:n.value]
+
+    def write_vtk(self, path, fmt=VTK_VTU_ASCII, fields=VTK_DESLOC | VTK_STRESS) -> int:
+        """write_mesh_res_mec: the result file at `path`; returns its size."""
+        n = C.c_int64(0)
+        self._check(self._L.elx_write_vtk(self._h, os.fsencode(path), fmt, fields, C.byref(n)))
+        return n.value
+
     def state(self):
         """The resident (u (nnode, ndf), b0 (neq,))."""
         m = self.mesh
@@ -453,6 +473,17 @@ def solv(ctx: Context, b, tol=1e-11, maxit=10000, ngram=50, solver=SOLVER_PCG,
          precision=PREC_FP64):
     """solv(neq,nad,...,b,x,tol,maxit,ngram,...,solver,...) (Solv.f:13-15)."""
     return ctx.solve(b, solver=solver, precision=precision, tol=tol, maxit=maxit, ngram=ngram)
+
+
+def fortran_e(x, w=15, d=5, e=0):
+    """The device formatter's Ew.d (e = 0) / Ew.dEe fields of x (strings)."""
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    out = C.create_string_buffer(max(x.size * w, 1))
+    st = load().elx_fortran_e(x.ctypes.data_as(_VP), x.size, w, d, e, C.cast(out, _VP))
+    if st != OK:
+        raise ElasticError(st, "elx_fortran_e failed")
+    raw = out.raw[:x.size * w].decode()
+    return [raw[i * w:(i + 1) * w] for i in range(x.size)]
 
 
 def pload(mesh, id_eq):

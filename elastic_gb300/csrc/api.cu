@@ -153,8 +153,9 @@ void upload_structure(elx_ctx *c, bool prederived) {
   release_block(c);
   c->tuned_width[0] = c->tuned_width[1] = 0;
   for (DBuf *v : {&c->node_count, &c->tstress, &c->tx0buf, &c->fbuf, &c->ld_node, &c->ld_ptr,
-                  &c->ld_ent, &c->ld_vec})
+                  &c->ld_ent, &c->ld_vec, &c->vtkbuf})
     c->release(*v);
+  c->have_stress = false;
   c->have_fp32 = 0;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
@@ -1024,7 +1025,7 @@ void elx_destroy(elx_ctx *c) {
                   &c->bia, &c->bja, &c->bt, &c->bval, &c->bval32, &c->sell_ptr, &c->sell_col,
                   &c->sell_val, &c->sell_val64,
                   &c->node_count, &c->tstress, &c->tx0buf, &c->fbuf, &c->ld_node, &c->ld_ptr,
-                  &c->ld_ent, &c->ld_vec,
+                  &c->ld_ent, &c->ld_vec, &c->vtkbuf,
                   &c->u, &c->b0, &c->b, &c->xs, &c->r, &c->p, &c->q, &c->m, &c->z,
                   &c->scal, &c->partials, &c->counters, &c->flags, &c->diag})
     c->release(*d);
@@ -1036,6 +1037,7 @@ void elx_destroy(elx_ctx *c) {
   if (c->h_scal) cudaFreeHost(c->h_scal);
   if (c->h_diag) cudaFreeHost(c->h_diag);
   if (c->h_flags) cudaFreeHost(c->h_flags);
+  if (c->vtk_host) cudaFreeHost(c->vtk_host);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -1352,10 +1354,102 @@ int elx_stress(elx_ctx *c, const double *u, const double *tx0, double *t) {
     ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost,
                              c->stream));
     c->sync();
+    c->have_stress = c->h_flags[0] == INT_MAX;
     if (c->h_flags[0] != INT_MAX)
       throw Error{ELX_ERR_BAD_DET, "non-positive Jacobian determinant in element " +
                                        std::to_string(c->h_flags[0])};
   });
+}
+
+// The result file (write_mesh_res_mec) formatted on the device into
+// c->vtkbuf; returns its size.
+int64_t format_vtk(elx_ctx *c, int format, int fields) {
+  require(c->have_structure, ELX_ERR_STATE, "write results after the structure is set");
+  require(format == 0 || format == 1, ELX_ERR_ARG,
+          "format: 0 (XML VTU ASCII) or 1 (legacy binary VTK)");
+  require((fields & ~3) == 0, ELX_ERR_ARG, "fields: 1 desloc, 2 stress");
+  require(!(fields & 2) || c->have_stress, ELX_ERR_STATE,
+          "stress output asked before elx_stress computed the nodal stresses");
+  const elx::Mesh &m = c->mesh;
+  int nnoel = 0, ctype = -1;
+  for (int el = 0; el < m.numel; el++) {
+    const int iel = m.ie[m.ix[(size_t)el * (m.nen + 1) + m.nen] - 1];
+    int nn, ct;
+    switch (iel) {
+      case elx::TRIA3_STRAIN: case elx::TRIA3_STRESS: nn = 3, ct = 5; break;
+      case elx::QUAD4_STRAIN: case elx::QUAD4_STRESS: nn = 4, ct = 9; break;
+      case elx::TETRA4: nn = 4, ct = 10; break;
+      default: nn = 8, ct = 12; break;
+    }
+    require(ctype < 0 || ct == ctype, ELX_ERR_ARG,
+            "the result writer takes meshes of one cell type (as the reference's)");
+    ctype = ct;
+    nnoel = nn;
+  }
+  const elx::VtkLayout L =
+      elx::vtk_layout(format, fields, m.nnode, m.numel, m.ndf, nnoel, ctype);
+  if (c->vtkbuf.bytes < (size_t)L.size) c->alloc(c->vtkbuf, (size_t)L.size);
+  elx::launch_vtk(L, c->vtkbuf.as<char>(), c->mesh_dev(), m.ndm == 2 ? 4 : 6, nnoel, ctype,
+                  c->u.as<double>(), c->tstress.as<double>(), c->stream);
+  c->launches += (int64_t)L.sections.size();
+  return L.size;
+}
+
+int elx_format_vtk(elx_ctx *c, int32_t format, int32_t fields, char *out, int64_t capacity,
+                   int64_t *bytes) {
+  return guarded(c, [&] {
+    require(bytes != nullptr, ELX_ERR_ARG, "null bytes");
+    const int64_t n = format_vtk(c, format, fields);
+    *bytes = n;
+    if (out) {
+      require(capacity >= n, ELX_ERR_ARG, "output buffer too small");
+      ELX_CUDA(cudaMemcpyAsync(out, c->vtkbuf.p, (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    }
+    c->sync();
+  });
+}
+
+int elx_write_vtk(elx_ctx *c, const char *path, int32_t format, int32_t fields,
+                  int64_t *bytes) {
+  return guarded(c, [&] {
+    require(path != nullptr, ELX_ERR_ARG, "null path");
+    const int64_t n = format_vtk(c, format, fields);
+    if (c->vtk_host_bytes < (size_t)n) {
+      if (c->vtk_host) cudaFreeHost(c->vtk_host);
+      c->vtk_host = nullptr;
+      c->vtk_host_bytes = 0;
+      ELX_CUDA(cudaMallocHost(&c->vtk_host, (size_t)n));
+      c->vtk_host_bytes = (size_t)n;
+    }
+    ELX_CUDA(cudaMemcpyAsync(c->vtk_host, c->vtkbuf.p, (size_t)n, cudaMemcpyDeviceToHost,
+                             c->stream));
+    c->sync();
+    FILE *f = std::fopen(path, "wb");
+    require(f != nullptr, ELX_ERR_ARG, "cannot open the output file");
+    const size_t w = std::fwrite(c->vtk_host, 1, (size_t)n, f);
+    const int cl = std::fclose(f);
+    require(w == (size_t)n && cl == 0, ELX_ERR_ARG, "short write of the output file");
+    if (bytes) *bytes = n;
+  });
+}
+
+int elx_fortran_e(const double *x, int32_t n, int32_t w, int32_t d, int32_t e, char *out) {
+  // a stand-alone test hook: no context, its own buffers on device 0's
+  // current device
+  if (!x || !out || n < 0 || w <= 0 || w > 40 || d < 1 || d > 9 || e < 0 || e > 4)
+    return ELX_ERR_ARG;
+  double *dx = nullptr;
+  char *dout = nullptr;
+  cudaError_t st = cudaMalloc(&dx, (size_t)n * 8 + 8);
+  if (st == cudaSuccess) st = cudaMalloc(&dout, (size_t)n * w + 8);
+  if (st == cudaSuccess) st = cudaMemcpy(dx, x, (size_t)n * 8, cudaMemcpyHostToDevice);
+  if (st == cudaSuccess) {
+    elx::launch_fortran_e(dx, n, w, d, e, dout, nullptr);
+    st = cudaMemcpy(out, dout, (size_t)n * w, cudaMemcpyDeviceToHost);
+  }
+  cudaFree(dx);
+  cudaFree(dout);
+  return st == cudaSuccess ? ELX_OK : ELX_ERR_CUDA;
 }
 
 int elx_solve_block(elx_ctx *c, int32_t nrhs, int32_t precision, double tol, int32_t maxit,

@@ -61,6 +61,11 @@ struct elx_ctx {
   DBuf node_count, tstress, tx0buf;
   // device loads: nodal loads f, edge-load lists and load vectors
   DBuf fbuf, ld_node, ld_ptr, ld_ent, ld_vec;
+  bool have_stress = false;  // tstress holds the last elx_stress result
+  // result writer: the formatted file on the device and its pinned copy
+  DBuf vtkbuf;
+  char *vtk_host = nullptr;
+  size_t vtk_host_bytes = 0;
   // BiCGSTAB (r0, t) and GMRES (Krylov basis, small dense arrays, state)
   DBuf r0v, tv, gbasis, garrays, gstate;
   // block PCG: multi-vectors of up to blk_cap columns, scalars, staging

@@ -207,6 +207,28 @@ void launch_stress(const MeshDev &m, const Segment &seg, const double *u, double
 void launch_stress_average(int nnode, int ntn, const int32_t *count, const double *tx0,
                            double *ts, cudaStream_t st);
 void launch_update(int64_t n, const int32_t *eq, const double *x, double *u, cudaStream_t st);
+// Result writer (vtk.cu): the file of write_mesh_res_mec as host text pieces
+// and fixed-width device sections, formatted on the GPU.
+struct VtkLayout {
+  struct Text {
+    int64_t off;
+    std::string s;
+  };
+  struct Section {
+    int kind;
+    int64_t off;
+    int count;
+  };
+  std::vector<Text> texts;
+  std::vector<Section> sections;
+  int64_t size = 0;
+  void add_text(const std::string &s);
+  void add_section(int kind, int count, int nnoel, int ndf);
+};
+VtkLayout vtk_layout(int format, int fields, int nnode, int numel, int ndf, int nnoel, int ctype);
+void launch_vtk(const VtkLayout &L, char *dbuf, const MeshDev &m, int ntn, int nnoel, int ctype,
+                const double *u, const double *tx, cudaStream_t st);
+void launch_fortran_e(const double *x, int n, int w, int d, int e, char *out, cudaStream_t st);
 // Loads (loads.cu): pload_mec into the resident b0/u, then the 2-D edge
 // loads of pform_mec isw = 4 from host-built integer lists.
 constexpr int kEdgeEntryInts = 8;

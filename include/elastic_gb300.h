@@ -276,6 +276,26 @@ int elx_set_loads(elx_ctx *ctx, const double *f, const int32_t *eload,
                   const double *loadvec, int32_t nload);
 /* Copy the resident u(ndf,nnode) and b0(neq) to the host (either NULL). */
 int elx_get_state(elx_ctx *ctx, double *u, double *b0);
+
+/* Result writer: the file of write_mesh_res_mec (Write_vtk.f:742-985 with
+ * the record writers of Vtk.f), formatted on the GPU from the resident mesh,
+ * the resident u (fields & 1: "desloc", fprint(2)) and the nodal stresses of
+ * the last elx_stress call (fields & 2: "stress", fprint(3)).  format 0: the
+ * reference's default XML VTU ASCII file (legacy_vtk = bvtk = .false.);
+ * format 1: its legacy binary VTK file (legacy_vtk = bvtk = .true., big-
+ * endian).  Byte for byte the reference's records, numbers as gfortran
+ * prints the Ew.d[Ee] / Iw edit descriptors.  The mesh must be of one cell
+ * type (as the reference's writer assumes).  elx_write_vtk writes `path`;
+ * elx_format_vtk returns the size in *bytes and, if out != NULL, copies the
+ * file into out (capacity bytes).  ELX_ERR_STATE for stresses not yet
+ * computed. */
+int elx_write_vtk(elx_ctx *ctx, const char *path, int32_t format, int32_t fields,
+                  int64_t *bytes);
+int elx_format_vtk(elx_ctx *ctx, int32_t format, int32_t fields, char *out,
+                   int64_t capacity, int64_t *bytes);
+/* Test hook of the device number formatter: n fields Ew.d (e = 0) or
+ * Ew.dEe of x into out (n * w chars), as the writer prints them. */
+int elx_fortran_e(const double *x, int32_t n, int32_t w, int32_t d, int32_t e, char *out);
 int elx_assemble_resident(elx_ctx *ctx);
 int elx_solve_resident(elx_ctx *ctx, int32_t solver, int32_t precision,
                        double tol, int32_t maxit, int32_t ngram,

@@ -76,6 +76,10 @@ def lib():
                                 C.c_int, C.c_int, C.c_int, C.c_int, F64P, I32P,
                                 C.POINTER(C.c_int)]
         L.orc_update.argtypes = [I32P, F64P, F64P, C.c_int, C.c_int]
+        L.orc_write_mesh_res.argtypes = [C.c_char_p, C.c_int, I32P, I32P, F64P, C.c_void_p,
+                                         C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_int, C.c_int]
+        L.orc_fortran_e.argtypes = [F64P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p]
         L.orc_matvec_csrcsym1.argtypes = [C.c_int, I32P, I32P, F64P, F64P, F64P, F64P]
         L.orc_dot.restype = C.c_double
         L.orc_dot.argtypes = [F64P, F64P, C.c_int]
@@ -201,6 +205,29 @@ def tform(mesh, u, tx0=None):
     if st:
         raise OracleError(st, f"element {bad.value}")
     return t
+
+
+def write_mesh_res(path, mesh, u=None, t=None, fmt=0):
+    """write_mesh_res_mec (Write_vtk.f:742-985): the result file at `path`,
+    fmt 0 the XML VTU ASCII file, 1 the legacy binary VTK file; u (nnode,
+    ndf) -> "desloc", t (nnode, ntn) -> "stress"."""
+    ntn = 4 if mesh.ndm == 2 else 6
+    up = None if u is None else _f64(u).ctypes.data_as(C.c_void_p)
+    tp = None if t is None else _f64(t).ctypes.data_as(C.c_void_p)
+    st = lib().orc_write_mesh_res(os.fsencode(path), fmt, _i32(mesh.ix), _i32(mesh.ie),
+                                  _f64(mesh.x), up, tp, mesh.nnode, mesh.numel, mesh.nen,
+                                  mesh.ndm, mesh.ndf, ntn)
+    if st:
+        raise OracleError(st, "write_mesh_res")
+
+
+def fortran_e(x, w=15, d=5, e=0):
+    """Fortran Ew.d (e = 0) / Ew.dEe fields of x as gfortran prints them."""
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    out = C.create_string_buffer(max(x.size * w, 1))
+    lib().orc_fortran_e(x, x.size, w, d, e, out)
+    raw = out.raw[:x.size * w].decode()
+    return [raw[i * w:(i + 1) * w] for i in range(x.size)]
 
 
 def colormsh(mesh):

@@ -20,6 +20,7 @@
  * the algorithm, so an insertion sort with the same ascending order is used.
  */
 #include <math.h>
+#include <stdio.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1758,4 +1759,266 @@ int orc_max_threads(void) {
 #else
   return 1;
 #endif
+}
+
+/* ---------------------------------------------------------------------- */
+/* Write_vtk.f / Vtk.f -- the result file of write_mesh_res_mec            */
+/* ---------------------------------------------------------------------- */
+
+/* The Fortran edit descriptors the writer uses, as gfortran prints them:
+ * Ew.d / Ew.dEe -> [-]0.d1..dd followed by E+xx (Ee: E+ and e digits; no
+ * Ee and 99 < |x| <= 999: +xxx without the E), right-justified in w;
+ * digits correctly rounded (glibc's exact conversion, ties to even); zero
+ * prints exponent 0; NaN / Infinity right-justified; a field that does not
+ * fit is w asterisks.  Iw -> right-justified, asterisks on overflow. */
+static void orc_fmt_e(char *out, double x, int w, int d, int e) {
+  char body[64];
+  int n = 0;
+  if (isnan(x)) {
+    n = snprintf(body, sizeof body, "NaN");
+  } else if (isinf(x)) {
+    n = snprintf(body, sizeof body, "%s", x < 0 ? (w >= 9 ? "-Infinity" : "-Inf")
+                                                : (w >= 8 ? "Infinity" : "Inf"));
+  } else {
+    char dig[40];
+    int ex = 0;
+    const double a = fabs(x);
+    if (a == 0.0) {
+      for (int i = 0; i < d; i++) dig[i] = '0';
+      dig[d] = 0;
+    } else {
+      char tmp[64];
+      snprintf(tmp, sizeof tmp, "%.*e", d - 1, a); /* D.DDDDe+XX */
+      int k = 0;
+      for (const char *p = tmp; *p && *p != 'e'; p++)
+        if (*p != '.') dig[k++] = *p;
+      dig[k] = 0;
+      ex = atoi(strchr(tmp, 'e') + 1) + 1;
+    }
+    const int aex = ex < 0 ? -ex : ex;
+    char expo[16];
+    if (e == 0) {
+      if (aex <= 99) snprintf(expo, sizeof expo, "E%c%02d", ex < 0 ? '-' : '+', aex);
+      else if (aex <= 999) snprintf(expo, sizeof expo, "%c%03d", ex < 0 ? '-' : '+', aex);
+      else expo[0] = 0, n = -1;
+    } else {
+      int lim = 1;
+      for (int i = 0; i < e; i++) lim *= 10;
+      if (aex < lim) snprintf(expo, sizeof expo, "E%c%0*d", ex < 0 ? '-' : '+', e, aex);
+      else expo[0] = 0, n = -1;
+    }
+    if (n == 0)
+      n = snprintf(body, sizeof body, "%s0.%s%s", signbit(x) ? "-" : "", dig, expo);
+    if (n > w && n - 1 == w) { /* drop the optional leading zero */
+      char *z = strstr(body, "0.");
+      memmove(z, z + 1, strlen(z));
+      n -= 1;
+    }
+  }
+  if (n < 0 || n > w) {
+    memset(out, '*', w);
+    return;
+  }
+  memset(out, ' ', w - n);
+  memcpy(out + w - n, body, n);
+}
+
+static void orc_fmt_i(char *out, long long v, int w) {
+  char body[32];
+  int n = snprintf(body, sizeof body, "%lld", v);
+  if (n > w) {
+    memset(out, '*', w);
+    return;
+  }
+  memset(out, ' ', w - n);
+  memcpy(out + w - n, body, n);
+}
+
+/* Writes E15.5 / E15.5E3 / Iw fields for the tests of the device formatter:
+ * out gets n fields of width w (kind 0: Ew.d with e = 0; 1: Ew.dEe). */
+void orc_fortran_e(const double *x, int n, int w, int d, int e, char *out) {
+  for (int i = 0; i < n; i++) orc_fmt_e(out + (size_t)i * w, x[i], w, d, e);
+}
+
+static void put_be(FILE *f, const void *p, int bytes) {
+  unsigned char b[8];
+  memcpy(b, p, bytes);
+  for (int i = bytes - 1; i >= 0; i--) fputc(b[i], f);
+}
+static void put_be_i32(FILE *f, int32_t v) { put_be(f, &v, 4); }
+static void put_be_f64(FILE *f, double v) { put_be(f, &v, 8); }
+
+/* VTK cell type and node count of the reference's element types
+ * (elm_vtk / elm_vtu: TRIA3 5, QUAD4 9, TETRA4 10, HEXA8 12). */
+static int vtk_cell(int iel, int *nnoel) {
+  switch (iel) {
+    case 2: case 3: *nnoel = 3; return 5;
+    case 4: case 5: *nnoel = 4; return 9;
+    case 6: *nnoel = 4; return 10;
+    case 7: *nnoel = 8; return 12;
+  }
+  return -1;
+}
+
+/* make_full_tensor (Write_vtk.f:1166-1226): the 9 components of node i. */
+static void full_tensor(const double *tx, int ntn, int i, double *t9) {
+  const double *s = tx + (size_t)i * ntn;
+  if (ntn == 4) {
+    t9[0] = s[0]; t9[1] = s[3]; t9[2] = 0.0;
+    t9[3] = s[3]; t9[4] = s[1]; t9[5] = 0.0;
+    t9[6] = 0.0;  t9[7] = 0.0;  t9[8] = s[2];
+  } else {
+    t9[0] = s[0]; t9[1] = s[3]; t9[2] = s[5];
+    t9[3] = s[3]; t9[4] = s[1]; t9[5] = s[4];
+    t9[6] = s[5]; t9[7] = s[4]; t9[8] = s[2];
+  }
+}
+
+/* write_mesh_res_mec (Write_vtk.f:742-985) with fprint(2) = u != NULL and
+ * fprint(3) = tx != NULL: format 0 = the XML VTU ASCII file (legacy =
+ * .false., bvtk = .false.: head_vtu, coor_vtu, elm_vtu, cell_prop_vtu,
+ * point_prop_vtu), format 1 = the legacy binary file (legacy = .true.,
+ * bvtk = .true.: head_vtk, coor_vtk, elm_vtk, cell_prop_vtk,
+ * point_prop_vtk, big-endian stream).  All elements must be of one VTK
+ * cell type (the reference's offsets loop assumes it, Vtk.f:1051). */
+int orc_write_mesh_res(const char *path, int format, const int *ix, const int *ie,
+                       const double *x, const double *u, const double *tx, int nnode,
+                       int numel, int nen, int ndm, int ndf, int ntn) {
+  int nnoel = 0, ctype = -1;
+  for (int el = 0; el < numel; el++) {
+    int nn, ct = vtk_cell(ie[ix[(size_t)el * (nen + 1) + nen] - 1], &nn);
+    if (ct < 0 || (ctype >= 0 && ct != ctype)) return ORC_ERR_ARG;
+    ctype = ct;
+    nnoel = nn;
+  }
+  FILE *f = fopen(path, "wb");
+  if (!f) return ORC_ERR_ARG;
+  char fld[32];
+  if (format == 0) {
+    fputs("<?xml version=\"1.0\"?>\n", f);
+    fputs("<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"BigEndian\">\n", f);
+    fputs("<UnstructuredGrid>\n", f);
+    fprintf(f, "<Piece NumberOfPoints=\"%15d\" NumberOfCells=\"%15d\">\n", nnode, numel);
+    fputs("<Points>\n", f);
+    fputs("<DataArray type=\"Float64\" NumberOfComponents =\"3\" format=\"ascii\">\n", f);
+    for (int i = 0; i < nnode; i++) {
+      for (int j = 0; j < 3; j++) {
+        orc_fmt_e(fld, j < ndm ? x[(size_t)i * ndm + j] : 0.0, 15, 5, 0);
+        fwrite(fld, 1, 15, f);
+      }
+      fputc('\n', f);
+    }
+    fputs("</DataArray>\n</Points>\n", f);
+    fputs("<Cells> \n", f);
+    fputs("<DataArray type=\"Int32\" Name=\"connectivity\" format=\"ascii\">\n", f);
+    for (int el = 0; el < numel; el++) {
+      for (int a = 0; a < nnoel; a++) {
+        orc_fmt_i(fld, ix[(size_t)el * (nen + 1) + a] - 1, 10);
+        fwrite(fld, 1, 10, f);
+      }
+      fputc('\n', f);
+    }
+    fputs("</DataArray>\n", f);
+    fputs("<DataArray type=\"Int64\" Name=\"offsets\" format=\"ascii\">\n", f);
+    for (long long el = 1; el <= numel; el++) {
+      orc_fmt_i(fld, el * nnoel, 20);
+      fwrite(fld, 1, 20, f);
+      fputc('\n', f);
+    }
+    fputs("</DataArray>\n", f);
+    fputs("<DataArray type=\"UInt8\" Name=\"types\" format=\"ascii\">\n", f);
+    for (int el = 0; el < numel; el++) {
+      orc_fmt_i(fld, ctype, 3);
+      fwrite(fld, 1, 3, f);
+      fputc('\n', f);
+    }
+    fputs("</DataArray>\n</Cells>\n", f);
+    fputs("<CellData Scalars=\"scalars\">\n", f);
+    for (int pass = 0; pass < 2; pass++) {
+      fprintf(f, "<DataArray type=\"Int32\" NumberOfComponents=\"1\" Name=\"%s\" format=\"ascii\">\n",
+              pass == 0 ? "mat" : "elIdG");
+      for (int el = 0; el < numel; el++) {
+        orc_fmt_i(fld, pass == 0 ? ix[(size_t)el * (nen + 1) + nen] : el + 1, 9);
+        fwrite(fld, 1, 9, f);
+        fputc('\n', f);
+      }
+      fputs("</DataArray>\n", f);
+    }
+    fputs("</CellData>\n", f);
+    fputs("<PointData>\n", f);
+    fputs("<DataArray type=\"Int32\" NumberOfComponents=\" 1\" Name=\"noIdG\" format=\"ascii\">\n", f);
+    for (int i = 0; i < nnode; i++) {
+      orc_fmt_i(fld, i + 1, 10);
+      fwrite(fld, 1, 10, f);
+      fputc('\n', f);
+    }
+    fputs("</DataArray>\n", f);
+    if (u) {
+      fprintf(f, "<DataArray type=\"Float64\" NumberOfComponents=\"%2d\" Name=\"desloc\" format=\"ascii\">\n",
+              ndf);
+      for (int i = 0; i < nnode; i++) {
+        for (int j = 0; j < ndf; j++) {
+          orc_fmt_e(fld, u[(size_t)i * ndf + j], 15, 5, 3);
+          fwrite(fld, 1, 15, f);
+        }
+        fputc('\n', f);
+      }
+      fputs("</DataArray>\n", f);
+    }
+    if (tx) {
+      fputs("<DataArray type=\"Float64\" NumberOfComponents=\"9\" Name=\"stress\" format=\"ascii\">\n", f);
+      for (int i = 0; i < nnode; i++) {
+        double t9[9];
+        full_tensor(tx, ntn, i, t9);
+        for (int j = 0; j < 9; j++) {
+          orc_fmt_e(fld, t9[j], 15, 5, 3);
+          fwrite(fld, 1, 15, f);
+        }
+        fputc('\n', f);
+      }
+      fputs("</DataArray>\n", f);
+    }
+    fputs("</PointData>\n</Piece>\n</UnstructuredGrid>\n</VTKFile>\n", f);
+  } else {
+    fputs("# vtk DataFile Version 3.0\n", f);
+    fprintf(f, "%-30s", "Malha Res");
+    fputs("\nBINARY\n", f);
+    fputs("DATASET UNSTRUCTURED_GRID\n", f);
+    fprintf(f, "POINTS %15d double\n", nnode);
+    for (int i = 0; i < nnode; i++)
+      for (int j = 0; j < 3; j++) put_be_f64(f, j < ndm ? x[(size_t)i * ndm + j] : 0.0);
+    fprintf(f, "\nCELLS %15d%15d\n", numel, (nnoel + 1) * numel);
+    for (int el = 0; el < numel; el++) {
+      put_be_i32(f, nnoel);
+      for (int a = 0; a < nnoel; a++) put_be_i32(f, ix[(size_t)el * (nen + 1) + a] - 1);
+    }
+    fprintf(f, "\nCELL_TYPES %15d\n", numel);
+    for (int el = 0; el < numel; el++) put_be_i32(f, ctype);
+    fprintf(f, "\nCELL_DATA %8d\n", numel);
+    for (int pass = 0; pass < 2; pass++) {
+      fprintf(f, "SCALARS %-15s int%8d\n", pass == 0 ? "mat" : "elIdG", 1);
+      fputs("LOOKUP_TABLE default\n", f);
+      for (int el = 0; el < numel; el++)
+        put_be_i32(f, pass == 0 ? ix[(size_t)el * (nen + 1) + nen] : el + 1);
+    }
+    fprintf(f, "\n POINT_DATA %8d\n", nnode);
+    fprintf(f, " SCALARS %-15s int %6d\n", "noIdG", 1);
+    fputs(" LOOKUP_TABLE default \n", f);
+    for (int i = 0; i < nnode; i++) put_be_i32(f, i + 1);
+    if (u) {
+      fprintf(f, " VECTORS %-15s double\n", "desloc");
+      for (int i = 0; i < nnode; i++)
+        for (int j = 0; j < 3; j++) put_be_f64(f, j < ndm ? u[(size_t)i * ndf + j] : 0.0);
+    }
+    if (tx) {
+      fprintf(f, " TENSORS %-15s double\n", "stress");
+      for (int i = 0; i < nnode; i++) {
+        double t9[9];
+        full_tensor(tx, ntn, i, t9);
+        for (int j = 0; j < 9; j++) put_be_f64(f, t9[j]);
+      }
+    }
+  }
+  fclose(f);
+  return ORC_OK;
 }
