@@ -12,7 +12,7 @@ with the mesh, structure and load vectors already resident on the device;
 b in, x out) copied every step.  Sub-objects: `mixed` (the same step with
 the mixed-precision solver), `after_solve` (the device load step, stress
 recovery and the result file on the solution, against the oracle's stress
-recovery and writer), `block`
+recovery and writer; the product through 4 row-block partitions), `block`
 (16 load cases of the 96x96x48 plate) and `serve` (a served request stream
 against sequential plain FP64 solves).
 
@@ -300,10 +300,23 @@ def run_ours(args, dist: Dist):
         vtk_bytes = ctx.write_vtk(vtk_path)
         if k >= args.warmup:
             vt_s.append(time.perf_counter() - t)
+    # the partitioned product: 4 row blocks with their halo gathers (the data
+    # path of a 4-GPU run, all partitions on this GPU), against the single
+    # product timed above
+    ctx.partition_spmv_resident(4, 3)
+    torch.cuda.synchronize(dev)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(ext)
+    ctx.partition_spmv_resident(4, 20)
+    p1.record(ext)
+    torch.cuda.synchronize(dev)
+    part = {"nparts": 4, "ms": p0.elapsed_time(p1) / 20, "single_ms": spmv_ms,
+            "halo_equations": sum(ctx.partition_info(4, q)[2] for q in range(4))}
     nxt = {"loads_ms": 1e3 * statistics.median(ld_s), "loads_h2d_bytes": mesh.f.size * 8,
            "stress_ms": 1e3 * statistics.median(sr_s),
            "stress_d2h_bytes": stresses.size * 8, "elements": mesh.numel,
-           "vtk_ms": 1e3 * statistics.median(vt_s), "vtk_bytes": vtk_bytes}
+           "vtk_ms": 1e3 * statistics.median(vt_s), "vtk_bytes": vtk_bytes,
+           "partitioned_spmv": part}
 
     out = None
     if dist.rank == 0:

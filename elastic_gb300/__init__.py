@@ -141,6 +141,13 @@ def load():
         "elx_stress": (C.c_int, [_VP, _VP, _VP, _VP]),
         "elx_update_resident": (C.c_int, [_VP]),
         "elx_set_loads": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32]),
+        "elx_partition_spmv": (C.c_int, [_VP, C.c_int32, _VP, _VP]),
+        "elx_partition_spmv_resident": (C.c_int, [_VP, C.c_int32, C.c_int32]),
+        "elx_partition_info": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP, _VP, _VP]),
+        "elx_host_partition_sizes": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP, _VP, _VP, _VP,
+                                               _VP]),
+        "elx_host_partition_get": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP, _VP, _VP, _VP,
+                                             _VP, _VP, _VP]),
         "elx_write_vtk": (C.c_int, [_VP, C.c_char_p, C.c_int32, C.c_int32, _VP]),
         "elx_format_vtk": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP, C.c_int64, _VP]),
         "elx_fortran_e": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _VP]),
@@ -207,6 +214,52 @@ def host_structure(mesh, reorder: bool = True) -> StructureArrays:
     finally:
         L.elx_host_structure_destroy(h)
     return StructureArrays(perm, idm, ia, ja[:nad], neq, nad, 0)
+
+
+@dataclass
+class PartitionArrays:
+    eq0: int
+    neq: int
+    halo: np.ndarray
+    ia: np.ndarray
+    ja: np.ndarray
+    ia1: np.ndarray
+    ja1: np.ndarray
+    pos: np.ndarray
+    pos1: np.ndarray
+
+
+def host_partition(mesh, nparts: int, part: int, reorder: bool = True) -> PartitionArrays:
+    """Partition `part` of `nparts` row blocks of the library's host structure
+    (elx_host_partition_*): the reference's overlapping-partition CSRC with
+    its rectangular part, local numbering, halo and value positions."""
+    L = load()
+    h = _VP()
+    st = L.elx_host_structure_create(C.byref(h), mesh.ndm, mesh.ndf, mesh.nen, mesh.numel,
+                                     mesh.nnode, _i32(mesh.ix), _i32(mesh.ie), mesh.numat,
+                                     _i32(mesh.id), int(reorder))
+    if st != OK:
+        raise ElasticError(st, "host structure build failed")
+    try:
+        eq0, neq, nh = C.c_int32(), C.c_int32(), C.c_int32()
+        nad, nad1 = C.c_int64(), C.c_int64()
+        st = L.elx_host_partition_sizes(h, nparts, part, C.byref(eq0), C.byref(neq),
+                                        C.byref(nh), C.byref(nad), C.byref(nad1))
+        if st != OK:
+            raise ElasticError(st, "host partition failed")
+        n = neq.value
+        halo = np.zeros(max(nh.value, 1), np.int32)
+        ia, ia1 = np.zeros(n + 1, np.int32), np.zeros(n + 1, np.int32)
+        ja = np.zeros(max(nad.value, 1), np.int32)
+        ja1 = np.zeros(max(nad1.value, 1), np.int32)
+        pos = np.zeros(max(nad.value, 1), np.int64)
+        pos1 = np.zeros(max(nad1.value, 1), np.int64)
+        L.elx_host_partition_get(h, nparts, part, _ptr(halo), _ptr(ia), _ptr(ja), _ptr(ia1),
+                                 _ptr(ja1), _ptr(pos), _ptr(pos1))
+    finally:
+        L.elx_host_structure_destroy(h)
+    return PartitionArrays(eq0.value, n, halo[:nh.value], ia, ja[:nad.value], ia1,
+                           ja1[:nad1.value], pos[:nad.value], pos1[:nad1.value])
 
 
 class Context:
@@ -419,6 +472,24 @@ class Context:
         n = C.c_int64(0)
         self._check(self._L.elx_write_vtk(self._h, os.fsencode(path), fmt, fields, C.byref(n)))
         return n.value
+
+    def partition_spmv(self, x, nparts):
+        """y = K x formed through nparts row-block partitions (their halo
+        exchange and local products) on this device."""
+        neq, _, _ = self.sizes()
+        y = np.zeros(neq)
+        self._check(self._L.elx_partition_spmv(self._h, nparts, _ptr(_f64(x)), _ptr(y)))
+        return y
+
+    def partition_spmv_resident(self, nparts, reps=1):
+        self._check(self._L.elx_partition_spmv_resident(self._h, nparts, reps))
+
+    def partition_info(self, nparts, part):
+        """(eq0, neq, nhalo) of one device partition (equations)."""
+        a, b, h = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self._L.elx_partition_info(self._h, nparts, part, C.byref(a), C.byref(b),
+                                               C.byref(h)))
+        return a.value, b.value, h.value
 
     def state(self):
         """The resident (u (nnode, ndf), b0 (neq,))."""

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libelastic_gb300.so")
-SOURCES = ["api.cu", "assemble.cu", "spmv.cu", "krylov.cu", "krylov_ns.cu", "bcsr.cu", "block_pcg.cu", "server.cu", "stress.cu", "loads.cu", "vtk.cu", "structure.cpp"]
+SOURCES = ["api.cu", "assemble.cu", "spmv.cu", "krylov.cu", "krylov_ns.cu", "bcsr.cu", "block_pcg.cu", "server.cu", "stress.cu", "loads.cu", "vtk.cu", "partition.cu", "structure.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

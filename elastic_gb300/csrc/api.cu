@@ -156,6 +156,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
                   &c->ld_ent, &c->ld_vec, &c->vtkbuf})
     c->release(*v);
   c->have_stress = false;
+  release_partitions(c);
   c->have_fp32 = 0;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
@@ -1016,6 +1017,7 @@ void elx_destroy(elx_ctx *c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   c->drop_graphs();
+  release_partitions(c);
   for (DBuf *d : {&c->conn, &c->mat, &c->elnum, &c->slot, &c->x, &c->eq, &c->e, &c->ia, &c->ja,
                   &c->iat, &c->jat, &c->pt, &c->ja16, &c->jat16, &c->alt, &c->alt32,
                   &c->tile_tgt, &c->tile_out, &c->tgt_col, &c->tgt_start, &c->tpos,
@@ -1103,6 +1105,7 @@ int elx_build_structure(elx_ctx *c, const int32_t *bc, int32_t reorder) {
 
 struct elx_host_structure {
   elx::Structure s;
+  int ndf = 0;
   std::string err;
 };
 
@@ -1117,6 +1120,7 @@ int elx_host_structure_create(elx_host_structure **out, int32_t ndm, int32_t ndf
     check_mesh(ndm, ndf, nen, numel, nnode, ix, ie, numat, 3);
     fill_mesh(m, ndm, ndf, nen, numel, nnode, ix, x.data(), ie, e.data(), 3, numat);
     auto *h = new elx_host_structure();
+    h->ndf = ndf;
     build_host_structure(m, bc, reorder != 0, h->s);
     *out = h;
     return ELX_OK;
@@ -1125,6 +1129,54 @@ int elx_host_structure_create(elx_host_structure **out, int32_t ndm, int32_t ndf
   } catch (const std::bad_alloc &) {
     return ELX_ERR_OOM;
   }
+}
+
+namespace {
+int host_partition(const elx_host_structure *h, int32_t nparts, int32_t part,
+                   elx::Partition &p) {
+  if (!h || nparts < 1 || part < 0 || part >= nparts) return ELX_ERR_ARG;
+  try {
+    const std::vector<int32_t> b = elx::partition_bounds(h->s, h->ndf, nparts);
+    if (b.empty()) return ELX_ERR_ARG;
+    elx::build_partition(h->s, b[part], b[part + 1], p);
+    return ELX_OK;
+  } catch (const std::bad_alloc &) {
+    return ELX_ERR_OOM;
+  }
+}
+}  // namespace
+
+int elx_host_partition_sizes(const elx_host_structure *h, int32_t nparts, int32_t part,
+                             int32_t *eq0, int32_t *neq, int32_t *nhalo, int64_t *nad,
+                             int64_t *nad1) {
+  elx::Partition p;
+  const int st = host_partition(h, nparts, part, p);
+  if (st != ELX_OK) return st;
+  if (eq0) *eq0 = p.eq0;
+  if (neq) *neq = p.neq;
+  if (nhalo) *nhalo = (int32_t)p.halo.size();
+  if (nad) *nad = (int64_t)p.ja.size();
+  if (nad1) *nad1 = (int64_t)p.ja1.size();
+  return ELX_OK;
+}
+
+int elx_host_partition_get(const elx_host_structure *h, int32_t nparts, int32_t part,
+                           int32_t *halo, int32_t *ia, int32_t *ja, int32_t *ia1,
+                           int32_t *ja1, int64_t *pos, int64_t *pos1) {
+  elx::Partition p;
+  const int st = host_partition(h, nparts, part, p);
+  if (st != ELX_OK) return st;
+  auto put = [](auto *dst, const auto &v) {
+    if (dst) std::copy(v.begin(), v.end(), dst);
+  };
+  put(halo, p.halo);
+  put(ia, p.ia);
+  put(ja, p.ja);
+  put(ia1, p.ia1);
+  put(ja1, p.ja1);
+  put(pos, p.pos);
+  put(pos1, p.pos1);
+  return ELX_OK;
 }
 
 int elx_host_structure_sizes(const elx_host_structure *h, int32_t *neq, int64_t *nad) {
@@ -1430,6 +1482,41 @@ int elx_write_vtk(elx_ctx *c, const char *path, int32_t format, int32_t fields,
     const int cl = std::fclose(f);
     require(w == (size_t)n && cl == 0, ELX_ERR_ARG, "short write of the output file");
     if (bytes) *bytes = n;
+  });
+}
+
+int elx_partition_spmv(elx_ctx *c, int32_t nparts, const double *x, double *y) {
+  return guarded(c, [&] {
+    require(c->have_matrix, ELX_ERR_STATE, "no matrix");
+    require(x && y && nparts >= 1, ELX_ERR_ARG, "null x or y, or nparts < 1");
+    const size_t n = (size_t)c->s.neq;
+    ELX_CUDA(cudaMemcpyAsync(c->p.p, x, n * 8, cudaMemcpyHostToDevice, c->stream));
+    partition_product(c, nparts, c->p.as<double>(), c->q.as<double>());
+    ELX_CUDA(cudaMemcpyAsync(y, c->q.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    c->sync();
+  });
+}
+
+int elx_partition_spmv_resident(elx_ctx *c, int32_t nparts, int32_t reps) {
+  return guarded(c, [&] {
+    require(c->have_matrix, ELX_ERR_STATE, "no matrix");
+    require(nparts >= 1 && reps >= 0, ELX_ERR_ARG, "nparts < 1 or reps < 0");
+    for (int i = 0; i < reps; i++)
+      partition_product(c, nparts, c->p.as<double>(), c->q.as<double>());
+  });
+}
+
+int elx_partition_info(elx_ctx *c, int32_t nparts, int32_t part, int32_t *eq0, int32_t *neq,
+                       int32_t *nhalo) {
+  return guarded(c, [&] {
+    require(c->have_structure, ELX_ERR_STATE, "set the structure first");
+    require(part >= 0 && part < nparts, ELX_ERR_ARG, "part outside 0..nparts-1");
+    ensure_partitions(c, nparts);
+    const elx_ctx::DevPartition &d = c->parts[part];
+    const int B = c->s.bsize;
+    if (eq0) *eq0 = d.I0 * B;
+    if (neq) *neq = (d.I1 - d.I0) * B;
+    if (nhalo) *nhalo = d.nhb * B;
   });
 }
 

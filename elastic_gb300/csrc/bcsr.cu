@@ -483,6 +483,20 @@ void launch_copy_sell64(const CsrcDev &k, cudaStream_t st) {
   ELX_CUDA(cudaGetLastError());
 }
 
+void launch_sell64_local(int nb, int nslices, int bsize, const int32_t *sell_ptr,
+                         const int32_t *sell_col, const double *sval, const double *x,
+                         double *y, cudaStream_t st) {
+  if (nslices <= 0) return;
+  const int grid = std::max(1, std::min((nslices + 7) / 8, 1216));
+  if (bsize == 3)
+    sell_spmv_kernel<double, 3, 1, true, kEpiNone><<<grid, 256, 0, st>>>(
+        nb, nslices, sell_ptr, sell_col, sval, x, y, nullptr, nullptr, nullptr, nullptr, nullptr);
+  else
+    sell_spmv_kernel<double, 2, 2, true, kEpiNone><<<grid, 256, 0, st>>>(
+        nb, nslices, sell_ptr, sell_col, sval, x, y, nullptr, nullptr, nullptr, nullptr, nullptr);
+  ELX_CUDA(cudaGetLastError());
+}
+
 // The gather entry points route here when the matrix has node blocks.
 template <class T, int EPI>
 void launch_bcsr(const CsrcDev &k, const T *x, T *y, const T *w, PcgScalars *sc,

@@ -62,6 +62,16 @@ struct elx_ctx {
   // device loads: nodal loads f, edge-load lists and load vectors
   DBuf fbuf, ld_node, ld_ptr, ld_ent, ld_vec;
   bool have_stress = false;  // tstress holds the last elx_stress result
+  // row-block partitions of the node-block matrix (partition.cu): owned
+  // block rows [I0, I1) = slices [s0, s1) of the sliced copy, values at voff,
+  // local slice pointers and columns, halo blocks, the gathered x
+  struct DevPartition {
+    int32_t I0 = 0, I1 = 0, s0 = 0, s1 = 0, nhb = 0;
+    int64_t voff = 0;
+    DBuf sptr, scol, hb, xloc;
+  };
+  std::vector<DevPartition> parts;
+  int parts_n = 0;
   // result writer: the formatted file on the device and its pinned copy
   DBuf vtkbuf;
   char *vtk_host = nullptr;
@@ -189,6 +199,11 @@ void upload_structure(elx_ctx *c, bool prederived = false);
 void assemble_resident(elx_ctx *c);
 void build_preconditioner(elx_ctx *c);
 void release_block(elx_ctx *c);
+void ensure_sell64(elx_ctx *c);
+// Row-block partitions on one device (partition.cu).
+void ensure_partitions(elx_ctx *c, int nparts);
+void release_partitions(elx_ctx *c);
+void partition_product(elx_ctx *c, int nparts, const double *x, double *y);
 // Block PCG of nrhs load cases (api.cu); b, x column-major neq x nrhs.
 void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int width,
                  const double *b, double *x, elx_info *infos, bool device_ptrs);

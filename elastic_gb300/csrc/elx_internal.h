@@ -124,6 +124,19 @@ struct Structure {
 
 constexpr int kSliceRows = 32;
 
+// One row-block partition of the CSRC (structure.cpp): owned global
+// equations [eq0, eq0 + neq), local numbering owned 1..neq then the halo
+// (equations outside the block that owned rows couple to, ascending) from
+// neq + 1; the lower CSRC among owned equations (ia, ja) and the rectangular
+// part (ia1, ja1), 1-based as csrstruct(lower, right) lays them out
+// (Csr.f:13-305); pos / pos1: each entry's 0-based position in the global al.
+struct Partition {
+  int32_t eq0 = 0, neq = 0;
+  std::vector<int32_t> halo;
+  std::vector<int32_t> ia, ja, ia1, ja1;
+  std::vector<int64_t> pos, pos1;
+};
+
 // host structure routines (structure.cpp)
 void node_graph(const Mesh &m, std::vector<int32_t> &xadj, std::vector<int32_t> &adj);
 void rcm_order(int32_t n, const std::vector<int32_t> &xadj,
@@ -136,6 +149,8 @@ void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> 
 void derive_structure(const Mesh &m, Structure &s);
 void build_tiles(Structure &s, int tile_rows);
 void build_transpose(Structure &s);
+std::vector<int32_t> partition_bounds(const Structure &s, int ndf, int nparts);
+void build_partition(const Structure &s, int32_t eq0, int32_t eq1, Partition &p);
 void build_blocks(Structure &s, int bsize);
 
 // ------------------------------------------------------------- kernels
@@ -248,6 +263,11 @@ void launch_demote_blocks(const CsrcDev &k, cudaStream_t st);
 // FP32 sliced copy of k.bval (k.sell_val), FP64 sliced copy (k.sell_val64)
 void launch_demote_sell(const CsrcDev &k, cudaStream_t st);
 void launch_copy_sell64(const CsrcDev &k, cudaStream_t st);
+// y = K x with the sliced FP64 kernel on explicit arrays (a partition's
+// local slices; no dot product)
+void launch_sell64_local(int nb, int nslices, int bsize, const int32_t *sell_ptr,
+                         const int32_t *sell_col, const double *sval, const double *x,
+                         double *y, cudaStream_t st);
 // Two-sided gather SpMV: y = K x reading the lower part (ja, al) and the
 // upper part through the transposed copy (jat, alt); with sc != nullptr it
 // also forms (x, y) and alpha = d / (x, y).

@@ -614,3 +614,103 @@ void build_blocks(Structure &s, int bsize) {
 }
 
 }  // namespace elx
+
+namespace elx {
+
+// Row-block partitions of the RCM-ordered equations for a multi-GPU run, one
+// partition per GPU, in the layout of the reference's overlapping MPI
+// partitions (csrstruct with lower = right = .true., Csr.f:13-305).
+//
+// Cuts fall on node boundaries -- on multiples of kSliceRows nodes when the
+// matrix has node blocks, so that a partition's rows are whole slices of the
+// sliced copy -- and balance the full-row nonzeros (each owned row's lower,
+// diagonal and upper entries), as Matrix_partition.f:98-150 balances rows
+// between threads.  Returns the nparts + 1 cut equations (0-based), or an
+// empty vector if there are fewer cut units than partitions.
+std::vector<int32_t> partition_bounds(const Structure &s, int ndf, int nparts) {
+  const int32_t neq = s.neq;
+  // the first equation of every node that has equations, ascending
+  std::vector<int32_t> starts;
+  const int nnode = (int)(s.id.size() / ndf);
+  for (int n = 0; n < nnode; n++) {
+    int32_t first = INT32_MAX;
+    for (int j = 0; j < ndf; j++)
+      if (s.id[(size_t)n * ndf + j] > 0) first = std::min(first, s.id[(size_t)n * ndf + j] - 1);
+    if (first != INT32_MAX) starts.push_back(first);
+  }
+  std::sort(starts.begin(), starts.end());
+  // node blocks: every node with equations has all ndf of them
+  bool blocked = neq % ndf == 0 && (int64_t)starts.size() * ndf == neq;
+  const int unit = blocked ? kSliceRows : 1;
+  std::vector<int32_t> cuts;  // candidate cut equations (unit starts)
+  for (size_t k = 0; k < starts.size(); k += unit) cuts.push_back(starts[k]);
+  if ((int)cuts.size() < nparts || nparts < 1) return {};
+  // prefix sums of full-row counts: lower + diagonal + upper entries
+  std::vector<int64_t> w(neq + 1, 0);
+  for (int i = 0; i < neq; i++) w[i + 1] = (s.ia[i + 1] - s.ia[i]) + 1;
+  for (int64_t k = 0; k < s.nad; k++) w[s.ja[k]] += 1;  // column c: upper entry of row c
+  for (int i = 0; i < neq; i++) w[i + 1] += w[i];
+  std::vector<int32_t> b(1, 0);
+  size_t c = 1;
+  for (int p = 1; p < nparts; p++) {
+    const int64_t target = w[neq] * p / nparts;
+    // the first candidate at or past the target, leaving room for the rest
+    while (c < cuts.size() && w[cuts[c]] < target) c++;
+    const size_t limit = cuts.size() - (size_t)(nparts - p);
+    if (c > limit) c = limit;
+    b.push_back(cuts[c]);
+    c++;
+  }
+  b.push_back(neq);
+  return b;
+}
+
+void build_partition(const Structure &s, int32_t eq0, int32_t eq1, Partition &p) {
+  p.eq0 = eq0;
+  p.neq = eq1 - eq0;
+  p.halo.clear();
+  // the rectangular entries of each owned row: (global column, al position)
+  std::vector<std::vector<std::pair<int32_t, int64_t>>> right(p.neq);
+  p.ia.assign(p.neq + 1, 1);
+  p.ja.clear();
+  p.pos.clear();
+  for (int32_t i = eq0; i < eq1; i++) {
+    for (int32_t k = s.ia[i] - 1; k < s.ia[i + 1] - 1; k++) {
+      const int32_t col = s.ja[k] - 1;
+      if (col >= eq0) {
+        p.ja.push_back(col - eq0 + 1);
+        p.pos.push_back(k);
+      } else {
+        right[i - eq0].push_back({col, k});
+      }
+    }
+    p.ia[i - eq0 + 1] = (int32_t)p.ja.size() + 1;
+  }
+  // upper entries of owned rows outside the block: rows past it whose
+  // lower part has an owned column
+  for (int32_t r = eq1; r < s.neq; r++)
+    for (int32_t k = s.ia[r] - 1; k < s.ia[r + 1] - 1; k++) {
+      const int32_t col = s.ja[k] - 1;
+      if (col >= eq0 && col < eq1) right[col - eq0].push_back({r, k});
+    }
+  for (auto &r : right)
+    for (auto &e : r) p.halo.push_back(e.first);
+  std::sort(p.halo.begin(), p.halo.end());
+  p.halo.erase(std::unique(p.halo.begin(), p.halo.end()), p.halo.end());
+  p.ia1.assign(p.neq + 1, 1);
+  p.ja1.clear();
+  p.pos1.clear();
+  for (int32_t r = 0; r < p.neq; r++) {
+    auto &e = right[r];
+    std::sort(e.begin(), e.end());
+    for (auto &q : e) {
+      const int32_t h = (int32_t)(std::lower_bound(p.halo.begin(), p.halo.end(), q.first) -
+                                  p.halo.begin());
+      p.ja1.push_back(p.neq + 1 + h);
+      p.pos1.push_back(q.second);
+    }
+    p.ia1[r + 1] = (int32_t)p.ja1.size() + 1;
+  }
+}
+
+}  // namespace elx

@@ -137,6 +137,25 @@ int elx_host_structure_get(const elx_host_structure *h, int32_t *perm,
                            int32_t *id, int32_t *ia, int32_t *ja);
 void elx_host_structure_destroy(elx_host_structure *h);
 
+/* Row-block partitions for a multi-GPU run (one partition per GPU), in the
+ * layout of the reference's overlapping MPI partitions: csrstruct with
+ * lower = right = .true. (Csr.f:13-305) on the partition's local numbering
+ * -- owned equations 1..neq (global eq0+1 .. eq0+neq of the RCM order),
+ * then the halo (the equations outside the block that owned rows couple
+ * to, ascending) from neq+1.  ia(neq+1)/ja(nad): the lower CSRC among owned
+ * equations; ia1(neq+1)/ja1(nad1): the rectangular part (owned rows x halo
+ * columns) that matvec_csrcrsym1 (Matvec.f:1090-1191) reads; pos/pos1: each
+ * entry's 0-based position in the global al (the values); halo(nhalo):
+ * 0-based global equations.  Cuts on node boundaries (multiples of 32 nodes
+ * with node blocks), balancing full-row nonzeros.  Host only, no GPU.
+ * ELX_ERR_ARG if there are fewer cut units than nparts. */
+int elx_host_partition_sizes(const elx_host_structure *h, int32_t nparts, int32_t part,
+                             int32_t *eq0, int32_t *neq, int32_t *nhalo, int64_t *nad,
+                             int64_t *nad1);
+int elx_host_partition_get(const elx_host_structure *h, int32_t nparts, int32_t part,
+                           int32_t *halo, int32_t *ia, int32_t *ja, int32_t *ia1,
+                           int32_t *ja1, int64_t *pos, int64_t *pos1);
+
 /* Sizes and copies of the structure (any pointer may be NULL). */
 int elx_get_sizes(const elx_ctx *ctx, int32_t *neq, int64_t *nad,
                   int32_t *ncolors);
@@ -293,6 +312,20 @@ int elx_write_vtk(elx_ctx *ctx, const char *path, int32_t format, int32_t fields
                   int64_t *bytes);
 int elx_format_vtk(elx_ctx *ctx, int32_t format, int32_t fields, char *out,
                    int64_t capacity, int64_t *bytes);
+/* The partitioned product on one GPU: y = K x formed partition by partition
+ * as a multi-GPU run forms it (elx_host_partition_* gives the same cuts),
+ * each partition gathering its halo of x (the exchange) and multiplying its
+ * owned block rows with the sliced node-block kernel on its local numbering
+ * (owned + halo columns: matvec_csrcrsym1, Matvec.f:1090-1191).  Bitwise
+ * equal to elx_spmv's FP64 product.  Node blocks required.
+ * elx_partition_spmv_resident runs `reps` products on the resident vectors
+ * (for timing); elx_partition_info gives a partition's owned equations and
+ * halo size. */
+int elx_partition_spmv(elx_ctx *ctx, int32_t nparts, const double *x, double *y);
+int elx_partition_spmv_resident(elx_ctx *ctx, int32_t nparts, int32_t reps);
+int elx_partition_info(elx_ctx *ctx, int32_t nparts, int32_t part, int32_t *eq0,
+                       int32_t *neq, int32_t *nhalo);
+
 /* Test hook of the device number formatter: n fields Ew.d (e = 0) or
  * Ew.dEe of x into out (n * w chars), as the writer prints them. */
 int elx_fortran_e(const double *x, int32_t n, int32_t w, int32_t d, int32_t e, char *out);

@@ -80,6 +80,11 @@ def lib():
                                          C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_int, C.c_int]
         L.orc_fortran_e.argtypes = [F64P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_char_p]
+        L.orc_csr_right.argtypes = [I32P, I32P, I32P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    C.c_int, C.c_void_p, C.c_void_p,
+                                    C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+        L.orc_matvec_csrcrsym1.argtypes = [C.c_int, I32P, I32P, I32P, I32P, F64P, F64P, F64P,
+                                           F64P, F64P]
         L.orc_matvec_csrcsym1.argtypes = [C.c_int, I32P, I32P, F64P, F64P, F64P, F64P]
         L.orc_dot.restype = C.c_double
         L.orc_dot.argtypes = [F64P, F64P, C.c_int]
@@ -228,6 +233,39 @@ def fortran_e(x, w=15, d=5, e=0):
     lib().orc_fortran_e(x, x.size, w, d, e, out)
     raw = out.raw[:x.size * w].decode()
     return [raw[i * w:(i + 1) * w] for i in range(x.size)]
+
+
+def csr_right(mesh, local_id, perm, neq):
+    """csrstruct with lower = right = .true. (Csr.f:13-305) on a partition's
+    local equation numbers local_id (nnode, ndf; owned 1..neq, halo > neq,
+    0 elsewhere): (ia, ja, ia1, ja1), 1-based, both parts sorted per row."""
+    L = lib()
+    nad, nad1 = C.c_longlong(0), C.c_longlong(0)
+    lid = _i32(local_id)
+    st = L.orc_csr_right(lid, _i32(perm), _i32(mesh.ix), mesh.nnode, mesh.numel, mesh.nen,
+                         mesh.ndf, neq, None, None, C.byref(nad), C.byref(nad1))
+    if st:
+        raise OracleError(st, "csr_right")
+    ia = np.zeros(2 * neq + 2, np.int32)
+    ja = np.zeros(max(nad.value + nad1.value, 1), np.int32)
+    st = L.orc_csr_right(lid, _i32(perm), _i32(mesh.ix), mesh.nnode, mesh.numel, mesh.nen,
+                         mesh.ndf, neq, ia.ctypes.data_as(C.c_void_p),
+                         ja.ctypes.data_as(C.c_void_p), C.byref(nad), C.byref(nad1))
+    if st:
+        raise OracleError(st, "csr_right")
+    n = nad.value
+    return ia[:neq + 1], ja[:n], ia[neq + 1:], ja[n:n + nad1.value]
+
+
+def matvec_csrcrsym1(neq, ia, ja, ia1, ja1, ad, al, ar, x):
+    """matvec_csrcrsym1 (Matvec.f:1090-1191): y(neq) on a partition, x = the
+    owned then the halo values."""
+    y = np.zeros(neq)
+    z1 = lambda a, t: a if len(a) else np.zeros(1, t)
+    lib().orc_matvec_csrcrsym1(neq, _i32(ia), z1(_i32(ja), np.int32), _i32(ia1),
+                               z1(_i32(ja1), np.int32), _f64(ad), z1(_f64(al), np.float64),
+                               z1(_f64(ar), np.float64), _f64(x), y)
+    return y
 
 
 def colormsh(mesh):

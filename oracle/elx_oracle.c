@@ -403,6 +403,90 @@ static void csrja_lower(const int *id, const int *num, const int *ip,
   for (int i = 0; i < neq; i++) sort_asc(&ja[ia[i] - 1], ia[i + 1] - ia[i]);
 }
 
+/* Csr.f:87-305 csria / csrja with lower = right = .true. (an overlapping
+ * MPI partition: equations > neq are the halo).  ia gets 2 (neq + 1)
+ * entries: ia(1..neq+1) for the lower part, ia(neq+2..2neq+2) for the
+ * rectangular part (1-based positions from 1 into ja(nad+1..)); ja gets nad
+ * + nad1 columns; both parts sorted per row (sortgraph, Csr.f:81-84).
+ * With ja == NULL only the counts are returned. */
+int orc_csr_right(const int *id, const int *num, const int *ix, int nnode, int numel,
+                  int nen, int ndf, int neq, int *ia, int *ja, long long *nad_out,
+                  long long *nad1_out) {
+  int *ip, *adj;
+  int st = graph(ix, nnode, numel, nen, &ip, &adj);
+  if (st) return st;
+  int *c = (int *)calloc((size_t)2 * neq + 4, sizeof(int)); /* c[1..2neq+2] */
+  if (!c) return ORC_ERR_OOM;
+  for (int no = 1; no <= nnode; no++) {
+    int i = num[no - 1];
+    for (int ii = 1; ii <= ndf; ii++) {
+      int neqi = ID(ii, i);
+      if (!(neqi > 0 && neqi <= neq)) continue;
+      for (int kk = 1; kk <= ndf; kk++) {
+        int neqj = ID(kk, i);
+        if (neqj <= 0) continue;
+        if (neqj < neqi) c[neqi]++;
+      }
+      for (int k = ip[i]; k <= ip[i + 1] - 1; k++) {
+        int j = adj[k - 1];
+        for (int jj = 1; jj <= ndf; jj++) {
+          int neqj = ID(jj, j);
+          if (neqj <= 0) continue;
+          if (neqj < neqi) c[neqi]++;
+          else if (neqj > neq) c[neq + 1 + neqi]++;
+        }
+      }
+    }
+  }
+  for (int i = neq; i >= 1; i--) {
+    c[i + 1] = c[i];
+    c[i + neq + 2] = c[i + neq + 1];
+  }
+  c[1] = 1;
+  c[neq + 2] = 1;
+  for (int i = 1; i <= neq; i++) {
+    c[i + 1] += c[i];
+    c[i + neq + 2] += c[i + neq + 1];
+  }
+  const long long nad = (long long)c[neq + 1] - 1, nad1 = (long long)c[2 * neq + 2] - 1;
+  if (nad_out) *nad_out = nad;
+  if (nad1_out) *nad1_out = nad1;
+  if (ia)
+    for (int i = 1; i <= 2 * neq + 2; i++) ia[i - 1] = c[i];
+  if (ja) {
+    long long n = 0, m = 0;
+    for (int no = 1; no <= nnode; no++) {
+      int i = num[no - 1];
+      for (int ii = 1; ii <= ndf; ii++) {
+        int neqi = ID(ii, i);
+        if (!(neqi > 0 && neqi <= neq)) continue;
+        for (int kk = 1; kk <= ndf; kk++) {
+          int neqj = ID(kk, i);
+          if (neqj <= 0) continue;
+          if (neqj < neqi) ja[n++] = neqj;
+        }
+        for (int k = ip[i]; k <= ip[i + 1] - 1; k++) {
+          int j = adj[k - 1];
+          for (int jj = 1; jj <= ndf; jj++) {
+            int neqj = ID(jj, j);
+            if (neqj <= 0) continue;
+            if (neqj < neqi) ja[n++] = neqj;
+            else if (neqj > neq) ja[nad + m++] = neqj;
+          }
+        }
+      }
+    }
+    for (int i = 1; i <= neq; i++) {
+      sort_asc(&ja[c[i] - 1], c[i + 1] - c[i]);
+      sort_asc(&ja[nad + c[neq + 1 + i] - 1], c[neq + 2 + i] - c[neq + 1 + i]);
+    }
+  }
+  free(c);
+  free(ip);
+  free(adj);
+  return ORC_OK;
+}
+
 /* csrstruct phase 1: ia (neq+1 ints).  Returns nad (>= 0) or -status. */
 long long orc_csr_ia(const int *id, const int *num, const int *ix, int nnode,
                      int numel, int nen, int ndf, int neq, int *ia) {
@@ -1257,6 +1341,47 @@ void orc_matvec_csrcsym1(int neq, const int *ia, const int *ja,
         y[jak - 1] = y[jak - 1] + s * xi;
         y[jak1 - 1] = y[jak1 - 1] + s1 * xi;
       }
+    }
+    y[i - 1] = t;
+  }
+}
+
+/* Matvec.f:1090-1191 matvec_csrcrsym1: y = A x on an overlapping
+ * partition -- the lower CSRC part with its mirror as matvec_csrcsym1, then
+ * each owned row times the halo values through the rectangular part (ia1,
+ * ja1, ar), 2-way unrolled; x holds the owned then the halo values (the
+ * exchange, communicate(), has filled the halo). */
+void orc_matvec_csrcrsym1(int neq, const int *ia, const int *ja, const int *ia1,
+                          const int *ja1, const double *ad, const double *al,
+                          const double *ar, const double *x, double *y) {
+  for (int i = 1; i <= neq; i++) {
+    double xi = x[i - 1];
+    double t = ad[i - 1] * xi;
+    int k1 = ia[i - 1], k2 = ia[i];
+    if (k2 != k1) {
+      if ((k2 - k1) % 2 != 0) {
+        int jak1 = ja[k1 - 1];
+        t = t + al[k1 - 1] * x[jak1 - 1];
+        y[jak1 - 1] = y[jak1 - 1] + al[k1 - 1] * xi;
+        k1 = k1 + 1;
+      }
+      for (int k = k1; k <= k2 - 1; k += 2) {
+        int jak = ja[k - 1], jak1 = ja[k];
+        double s = al[k - 1], s1 = al[k];
+        t = t + s * x[jak - 1] + s1 * x[jak1 - 1];
+        y[jak - 1] = y[jak - 1] + s * xi;
+        y[jak1 - 1] = y[jak1 - 1] + s1 * xi;
+      }
+    }
+    k1 = ia1[i - 1];
+    k2 = ia1[i];
+    if (k2 != k1) {
+      if ((k2 - k1) % 2 != 0) {
+        t = t + ar[k1 - 1] * x[ja1[k1 - 1] - 1];
+        k1 = k1 + 1;
+      }
+      for (int k = k1; k <= k2 - 1; k += 2)
+        t = t + ar[k - 1] * x[ja1[k - 1] - 1] + ar[k] * x[ja1[k] - 1];
     }
     y[i - 1] = t;
   }
