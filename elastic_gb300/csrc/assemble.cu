@@ -26,6 +26,9 @@
 // d11, d12, d22, d33 (Elmlib02.f:781-795).  Rounding differs from the
 // reference's operand order by a few ulps; the assembled values agree to
 // well below 1e-13 relative.
+#include <cstdlib>
+#include <mutex>
+
 #include "elx_internal.h"
 
 namespace elx {
@@ -471,6 +474,218 @@ hexa8_kernel(MeshDev m, CsrcDev k, int begin, int end, const double *__restrict_
 #undef SG
 }
 
+// HEXA8 with a team of 8 threads per element.  One thread per element
+// (hexa8_kernel, ELX_HEX_TEAM=0) left each colour's launch with 32,768 long
+// serial threads on the 64^3 cube: 8.45 ms per assembly, latency bound.
+// Here thread g of a team first forms integration point g (Jacobian, one
+// reciprocal of its determinant, the 8 nodes' gradients and weighted
+// gradients into shared memory; the natural derivatives come from a table)
+// and stages node g's equations and displacements, then the team splits the
+// 36 node pairs (lane i: pairs i, i+8, ...), each pair's block formed as in
+// hexa8_kernel; the element vector K u is summed over the team by a fixed
+// shuffle tree and lane g subtracts node g's part from b.  5.30 ms per
+// assembly, the FP64 pipe 77 % busy (FP64-bound: ~7,000 FP64 operations per
+// element).
+constexpr int kTeamElems = 8;  // elements per 64-thread block
+
+// Natural derivatives (d/dr, d/ds, d/dt) of the 8 shape functions at the 8
+// points (sfhexa8_m, Elmlib.f:1151-1258; point g = lx + 2 ly + 4 lz), the
+// same for every element: filled once from the host with the kernel's own
+// expressions (exact: the node signs are +-1 and 0.125 a power of two).
+__device__ __constant__ double kHexDh[8][3][8];
+
+__device__ __constant__ unsigned char kPairA[36] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 4, 4,
+                                                    4, 4, 4, 5, 5, 5, 5, 5, 5, 6, 6, 6,
+                                                    6, 6, 6, 6, 7, 7, 7, 7, 7, 7, 7, 7};
+__device__ __constant__ unsigned char kPairB[36] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1,
+                                                    2, 3, 4, 0, 1, 2, 3, 4, 5, 0, 1, 2,
+                                                    3, 4, 5, 6, 0, 1, 2, 3, 4, 5, 6, 7};
+
+__global__ void __launch_bounds__(64)
+hexa8_team_kernel(MeshDev m, CsrcDev k, int begin, int end, const double *__restrict__ u,
+                  double *__restrict__ b, int32_t *bad) {
+  __shared__ double sg[kTeamElems][8][8][3];   // [element][point][node][d]: gradients
+  __shared__ double swg[kTeamElems][8][8][3];  // the same times the point's weight
+  __shared__ double su[kTeamElems][8][3];
+  __shared__ int seq[kTeamElems][8][3];
+  __shared__ int sfirst[kTeamElems][8];
+  const int le = threadIdx.x >> 3, lane = threadIdx.x & 7;
+  const int t = begin + blockIdx.x * kTeamElems + le;
+  const bool active = t < end;
+  const int te = active ? t : begin;  // inactive teams read a valid element, write nothing
+  int node[8];
+#pragma unroll
+  for (int a = 0; a < 8; a++) node[a] = m.conn[(size_t)a * m.numel + te];
+  const Law L = make_law(HEXA8, m.e + (size_t)m.mat[te] * m.prop);
+  {
+    // integration point `lane`
+    double hr[8], hs[8], ht[8];
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      hr[a] = kHexDh[lane][0][a];
+      hs[a] = kHexDh[lane][1][a];
+      ht[a] = kHexDh[lane][2][a];
+    }
+    double xj[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const double xa = m.x[(size_t)node[a] * 3 + d];
+        xj[0][d] += hr[a] * xa;
+        xj[1][d] += hs[a] * xa;
+        xj[2][d] += ht[a] * xa;
+      }
+    const double det = xj[0][0] * xj[1][1] * xj[2][2] + xj[0][1] * xj[1][2] * xj[2][0] +
+                       xj[0][2] * xj[1][0] * xj[2][1] - xj[2][0] * xj[1][1] * xj[0][2] -
+                       xj[1][0] * xj[0][1] * xj[2][2] - xj[0][0] * xj[2][1] * xj[1][2];
+    if (active && det <= 1.e-14) mark_bad(bad, m.elnum[t]);
+    // the inverse Jacobian through one reciprocal of det (one FP64 division
+    // instead of nine; the FP64 pipe bounds this kernel)
+    const double rd = 1.0 / det;
+    double ji[3][3];
+    ji[0][0] = (xj[1][1] * xj[2][2] - xj[1][2] * xj[2][1]) * rd;
+    ji[1][0] = -(xj[1][0] * xj[2][2] - xj[1][2] * xj[2][0]) * rd;
+    ji[2][0] = (xj[1][0] * xj[2][1] - xj[1][1] * xj[2][0]) * rd;
+    ji[0][1] = -(xj[0][1] * xj[2][2] - xj[0][2] * xj[2][1]) * rd;
+    ji[1][1] = (xj[0][0] * xj[2][2] - xj[0][2] * xj[2][0]) * rd;
+    ji[2][1] = -(xj[0][0] * xj[2][1] - xj[0][1] * xj[2][0]) * rd;
+    ji[0][2] = (xj[0][1] * xj[1][2] - xj[0][2] * xj[1][1]) * rd;
+    ji[1][2] = -(xj[0][0] * xj[1][2] - xj[0][2] * xj[1][0]) * rd;
+    ji[2][2] = (xj[0][0] * xj[1][1] - xj[0][1] * xj[1][0]) * rd;
+    const double w = det * L.a;  // wg^3 = 1
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const double g = ji[d][0] * hr[a] + ji[d][1] * hs[a] + ji[d][2] * ht[a];
+        sg[le][lane][a][d] = g;
+        swg[le][lane][a][d] = w * g;
+      }
+    // node `lane`: its equations, the smallest of them, its displacements
+    int f = -1;
+#pragma unroll
+    for (int d = 2; d >= 0; d--) {
+      const int q = m.eq[(size_t)node[lane] * 3 + d];
+      seq[le][lane][d] = q;
+      if (q >= 0) f = q;
+      su[le][lane][d] = u ? u[(size_t)node[lane] * 3 + d] : 0.0;
+    }
+    sfirst[le][lane] = f;
+  }
+  __syncthreads();
+  const bool with_u = u != nullptr;
+  double p[8][3];
+#pragma unroll
+  for (int a = 0; a < 8; a++)
+#pragma unroll
+    for (int d = 0; d < 3; d++) p[a][d] = 0.0;
+  for (int q = lane; q < 36; q += 8) {
+    const int a = kPairA[q], bb = kPairB[q];
+    double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, K[3][3];
+#pragma unroll
+    for (int gp = 0; gp < 8; gp++) {
+      const double s0 = swg[le][gp][a][0], s1 = swg[le][gp][a][1], s2 = swg[le][gp][a][2];
+      const double g0 = sg[le][gp][bb][0], g1 = sg[le][gp][bb][1], g2 = sg[le][gp][bb][2];
+      M[0][0] += s0 * g0; M[0][1] += s0 * g1; M[0][2] += s0 * g2;
+      M[1][0] += s1 * g0; M[1][1] += s1 * g1; M[1][2] += s1 * g2;
+      M[2][0] += s2 * g0; M[2][1] += s2 * g1; M[2][2] += s2 * g2;
+    }
+    block3d(L, M, K);
+    if (with_u) {
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          p[a][r] += K[r][c] * su[le][bb][c];
+          if (a != bb) p[bb][c] += K[r][c] * su[le][a][r];
+        }
+    }
+    if (!active) continue;
+    if (a == bb) {
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        const int row = seq[le][a][r];
+        if (row < 0) continue;
+        k.ad[row] += K[r][r];
+        const int endr = k.ia[row + 1];
+#pragma unroll
+        for (int c = 0; c < r; c++) {
+          const int col = seq[le][a][c];
+          if (col >= 0) k.al[endr - (row - col)] += K[r][c];
+        }
+      }
+    } else {
+      const int fa = sfirst[le][a], fb = sfirst[le][bb];
+      if (fa < 0 || fb < 0) continue;
+      const int off = m.slot[(size_t)pair_index(m.nen, bb, a) * m.numel + t];
+      if (fa > fb) {  // rows of a, columns of bb
+#pragma unroll
+        for (int r = 0; r < 3; r++) {
+          const int row = seq[le][a][r];
+          if (row < 0) continue;
+          const int base = k.ia[row] + off - fb;
+#pragma unroll
+          for (int c = 0; c < 3; c++)
+            if (seq[le][bb][c] >= 0) k.al[base + seq[le][bb][c]] += K[r][c];
+        }
+      } else {  // rows of bb, columns of a: entry (bb c, a r) = K[r][c]
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const int row = seq[le][bb][c];
+          if (row < 0) continue;
+          const int base = k.ia[row] + off - fa;
+#pragma unroll
+          for (int r = 0; r < 3; r++)
+            if (seq[le][a][r] >= 0) k.al[base + seq[le][a][r]] += K[r][c];
+        }
+      }
+    }
+  }
+  if (!with_u || b == nullptr) return;
+  // K u over the team: fixed shuffle tree within the 8 lanes
+#pragma unroll
+  for (int off = 4; off > 0; off >>= 1)
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+      for (int d = 0; d < 3; d++) p[a][d] += __shfl_xor_sync(0xffffffffu, p[a][d], off, 8);
+  if (!active) return;
+#pragma unroll
+  for (int a = 0; a < 8; a++)
+    if (a == lane)
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+        if (seq[le][a][d] >= 0) b[seq[le][a][d]] -= p[a][d];
+}
+
+// kHexDh for the current device, once per device.
+void fill_hex_table(cudaStream_t st) {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  ELX_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev < 0 || dev >= 64 || done[dev]) return;
+  static const double rn[8] = {1, -1, -1, 1, 1, -1, -1, 1};
+  static const double sn[8] = {1, 1, -1, -1, 1, 1, -1, -1};
+  static const double tn[8] = {1, 1, 1, 1, -1, -1, -1, -1};
+  static const double pg[2] = {-.577350269189626e0, .577350269189626e0};
+  static double h[8][3][8];
+  for (int g = 0; g < 8; g++) {
+    const double r = pg[g & 1], s = pg[(g >> 1) & 1], t = pg[g >> 2];
+    for (int a = 0; a < 8; a++) {
+      const double fr = 1.0 + rn[a] * r, fs = 1.0 + sn[a] * s, ft = 1.0 + tn[a] * t;
+      h[g][0][a] = rn[a] * (fs * ft * 0.125);
+      h[g][1][a] = sn[a] * (fr * ft * 0.125);
+      h[g][2][a] = tn[a] * (fr * fs * 0.125);
+    }
+  }
+  ELX_CUDA(cudaMemcpyToSymbolAsync(kHexDh, h, sizeof(h), 0, cudaMemcpyHostToDevice, st));
+  ELX_CUDA(cudaStreamSynchronize(st));
+  done[dev] = true;
+}
+
 }  // namespace
 
 void launch_assembly(const MeshDev &m, const CsrcDev &k, const Segment &seg,
@@ -490,10 +705,17 @@ void launch_assembly(const MeshDev &m, const CsrcDev &k, const Segment &seg,
       tetra4_kernel<<<(n + 127) / 128, 128, 0, st>>>(m, k, seg.begin, seg.end, u, b, bad);
       break;
     case HEXA8: {
-      ELX_CUDA(cudaFuncSetAttribute(hexa8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)kHexSmem));
-      hexa8_kernel<<<(n + kHexThreads - 1) / kHexThreads, kHexThreads, kHexSmem, st>>>(
-          m, k, seg.begin, seg.end, u, b, bad);
+      static const bool team = !getenv("ELX_HEX_TEAM") || atoi(getenv("ELX_HEX_TEAM")) != 0;
+      if (team) {
+        fill_hex_table(st);
+        hexa8_team_kernel<<<(n + kTeamElems - 1) / kTeamElems, 8 * kTeamElems, 0, st>>>(
+            m, k, seg.begin, seg.end, u, b, bad);
+      } else {
+        ELX_CUDA(cudaFuncSetAttribute(hexa8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)kHexSmem));
+        hexa8_kernel<<<(n + kHexThreads - 1) / kHexThreads, kHexThreads, kHexSmem, st>>>(
+            m, k, seg.begin, seg.end, u, b, bad);
+      }
       break;
     }
     default:
