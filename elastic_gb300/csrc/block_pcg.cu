@@ -23,7 +23,10 @@
 #include <algorithm>
 #include <type_traits>
 
+#include <cstdlib>
+
 #include "elx_krylov.h"
+#include "elx_ptx.cuh"
 #include "elx_reduce.cuh"
 
 namespace elx {
@@ -134,6 +137,23 @@ template <class T, int VC>
 struct ColVec {
   T v[VC];
 };
+// 16-byte column loads issued in program order (volatile; see spmm_kernel)
+template <class T, int VC>
+__device__ __forceinline__ ColVec<T, VC> load_cols_ordered(const T *p) {
+  ColVec<T, VC> r;
+  if constexpr (VC * sizeof(T) == 16 && sizeof(T) == 4) {
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3])
+                 : "l"(p));
+  } else if constexpr (VC * sizeof(T) == 16) {
+    asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(r.v[0]), "=d"(r.v[1]) : "l"(p));
+  } else {
+#pragma unroll
+    for (int j = 0; j < VC; j++) r.v[j] = ptx::ld_nc_ordered(p + j);
+  }
+  return r;
+}
+
 template <class T, int VC>
 __device__ __forceinline__ ColVec<T, VC> load_cols(const T *p) {
   ColVec<T, VC> r;
@@ -209,7 +229,7 @@ __device__ __forceinline__ bool column_reduce_v(double (&v)[VC], double *partial
 // address in all G lanes); every value then feeds VC FMAs per lane.  With
 // DOT, also pq_c = (x_c, y_c) and alpha_c = d_c / pq_c for the active
 // columns.  A launch with gate != nullptr runs only while *gate != 0.
-template <class T, int B, int W, bool DOT, bool MASK = false>
+template <class T, int B, int W, bool DOT, bool MASK = false, int U = 1>
 __global__ void __launch_bounds__(kThreads)
 spmm_kernel(int nb, const int32_t *__restrict__ bia, const int32_t *__restrict__ bja,
             const T *__restrict__ bval, const T *__restrict__ X, T *__restrict__ Y,
@@ -239,7 +259,37 @@ spmm_kernel(int nb, const int32_t *__restrict__ bia, const int32_t *__restrict__
     for (int a = 0; a < B; a++)
 #pragma unroll
       for (int j = 0; j < VC; j++) acc[a][j] = T(0);
-    for (int p = pb; p < pe; p++) {
+    // U blocks per step, all their loads issued before their FMAs (the
+    // FMAs keep the one-block order: the same sums bitwise)
+    int p = pb;
+    for (; p + U <= pe; p += U) {
+      int J[U];
+      T bv[U][BB];
+      ColVec<T, VC> xv[U][B];
+#pragma unroll
+      for (int u = 0; u < U; u++) J[u] = U > 1 ? ptx::ld_nc_ordered(bja + p + u) : bja[p + u];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int e = 0; e < BB; e++)
+          bv[u][e] = U > 1 ? ptx::ld_nc_ordered(bval + (size_t)(p + u) * BB + e)
+                           : bval[(size_t)(p + u) * BB + e];
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int b = 0; b < B; b++)
+          xv[u][b] = U > 1 ? load_cols_ordered<T, VC>(X + (size_t)(J[u] * B + b) * W + c0)
+                           : load_cols<T, VC>(X + (size_t)(J[u] * B + b) * W + c0);
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int a = 0; a < B; a++)
+#pragma unroll
+          for (int b = 0; b < B; b++)
+#pragma unroll
+            for (int j = 0; j < VC; j++) acc[a][j] += bv[u][a * B + b] * xv[u][b].v[j];
+    }
+    for (; p < pe; p++) {
       const int J = bja[p];
       T bv[BB];
 #pragma unroll
@@ -670,12 +720,17 @@ void spmm_w(const CsrcDev &k, const T *val, const T *X, T *Y, ColScalars *cols, 
     return;
   }
   if (k.bsize == 3) {
+    // 3 blocks in flight per step: 320 against 342 (2) and 339 (1) us for
+    // the W = 16 FP32 product with its dots on the 96x96x48 plate; 29.8
+    // against 31.1 and 33.6 ms per load case for the whole block solve
+#define ELX_SPMM(DOT_, U_)                                                                  \
+  spmm_kernel<T, 3, W, DOT_, false, U_><<<grid, kThreads, 0, st>>>(                          \
+      k.nb, k.bia, k.bja, val, X, Y, cols, hdr, partials, counter, gate)
     if (dot)
-      spmm_kernel<T, 3, W, true><<<grid, kThreads, 0, st>>>(k.nb, k.bia, k.bja, val, X, Y, cols,
-                                                            hdr, partials, counter, gate);
+      ELX_SPMM(true, 3);
     else
-      spmm_kernel<T, 3, W, false><<<grid, kThreads, 0, st>>>(k.nb, k.bia, k.bja, val, X, Y, cols,
-                                                             hdr, partials, counter, gate);
+      ELX_SPMM(false, 3);
+#undef ELX_SPMM
   } else {
     if (dot)
       spmm_kernel<T, 2, W, true><<<grid, kThreads, 0, st>>>(k.nb, k.bia, k.bja, val, X, Y, cols,
@@ -775,10 +830,12 @@ void launch_block_diagnostics(const CsrcDev &k, const BlockVecs &v, double *out,
 #undef CALL
 }
 
+// The autotuner's products: the solver's own form (with the fused (p, q)
+// dots), on the block vectors before the solve initialises its scalars.
 void launch_spmm32(const CsrcDev &k, const BlockVecs &v, cudaStream_t st) {
 #define CALL(W)                                                                                \
   spmm_w<float, W>(k, k.bval32, v.p32, v.q32, v.cols, v.hdr_on, v.partials, v.counters + 6, \
-                   nullptr, false, st)
+                   nullptr, true, st)
   ELX_W_DISPATCH(v.w, CALL)
 #undef CALL
   ELX_CUDA(cudaGetLastError());
@@ -787,7 +844,7 @@ void launch_spmm32(const CsrcDev &k, const BlockVecs &v, cudaStream_t st) {
 void launch_spmm64(const CsrcDev &k, const BlockVecs &v, cudaStream_t st) {
 #define CALL(W)                                                                            \
   spmm_w<double, W>(k, k.bval, v.p, v.q, v.cols, v.hdr_on, v.partials, v.counters + 6, \
-                    nullptr, false, st)
+                    nullptr, true, st)
   ELX_W_DISPATCH(v.w, CALL)
 #undef CALL
   ELX_CUDA(cudaGetLastError());

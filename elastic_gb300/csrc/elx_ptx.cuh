@@ -130,5 +130,26 @@ __device__ __forceinline__ int32_t ld_stream(const int32_t *p) {
   return v;
 }
 
+// Read-only loads issued in program order (volatile) but cached as usual:
+// for data that lanes of a warp share (the same block read by the lane
+// group of a row) and that should be in flight as a group.
+__device__ __forceinline__ float ld_nc_ordered(const float *p) {
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ double ld_nc_ordered(const double *p) {
+  double v;
+  asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ int32_t ld_nc_ordered(const int32_t *p) {
+  int32_t v;
+  asm volatile("ld.global.nc.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
 }  // namespace ptx
 }  // namespace elx
