@@ -21,10 +21,9 @@ from dataclasses import dataclass
 import numpy as np
 
 __all__ = ["ElasticError", "Context", "Server", "Info", "load", "library_path", "pform_mec",
-           "solv",
-           "host_structure",
+           "solv", "pload", "edge_loads", "host_structure", "host_partition", "fortran_e",
            "solvm", "SOLVER_PCG", "SOLVER_GMRES", "SOLVER_BICGSTAB", "PREC_FP64",
-           "PREC_MIXED"]
+           "PREC_MIXED", "VTK_VTU_ASCII", "VTK_LEGACY_BINARY", "VTK_DESLOC", "VTK_STRESS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libelastic_gb300.so")
