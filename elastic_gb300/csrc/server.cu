@@ -50,45 +50,48 @@ struct SlotScalars {
 };
 
 struct SlotDesc {
-  const int32_t *bia, *bja;
-  const double *bval, *m;
+  const int32_t *sell_ptr, *sell_col;  // the request's sliced FP64 node blocks
+  const double *sval, *m;
   double *x, *r, *p, *q;
   SlotScalars *sc;
-  int32_t bsize, n;
-  int32_t cta0, ncta;  // this slot's blocks in the packed launch
+  int32_t bsize, n, nb;
+  int32_t cta0, ncta;    // this slot's blocks in the packed vector launches
+  int32_t scta0, sncta;  // and in the packed product (8 slices per block)
 };
 
 namespace {
 
 constexpr int kRowsPerCta = kThreads;  // one row per thread
 
+// The slot of a block: cta0 (vector launches) or scta0 (the product).
+template <bool PRODUCT>
 __device__ __forceinline__ int find_slot(const SlotDesc *d, int nslots, int cta) {
   int lo = 0, hi = nslots - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (d[mid].cta0 <= cta) lo = mid; else hi = mid - 1;
+    if ((PRODUCT ? d[mid].scta0 : d[mid].cta0) <= cta) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
 
 // The slot's last block to arrive adds the slot's block partials in order;
 // returns true in that block (all threads), with the total in thread 0.
-__device__ __forceinline__ bool slot_reduce(double v, const SlotDesc &D, int phase,
-                                            double *partials, double &tot) {
+__device__ __forceinline__ bool slot_reduce(double v, const SlotDesc &D, int cta0, int ncta,
+                                            int phase, double *partials, double &tot) {
   double vv[1] = {v};
   block_sum<1>(vv);
   __shared__ bool last;
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = vv[0];
     __threadfence();
-    last = atomicAdd(&D.sc->ticket[phase], 1u) == (unsigned)D.ncta - 1;
+    last = atomicAdd(&D.sc->ticket[phase], 1u) == (unsigned)ncta - 1;
   }
   __syncthreads();
   if (!last) return false;
   __threadfence();
   double t[1] = {0.0};
 #pragma unroll 4
-  for (int b = threadIdx.x; b < D.ncta; b += kThreads) t[0] += __ldcg(partials + D.cta0 + b);
+  for (int b = threadIdx.x; b < ncta; b += kThreads) t[0] += __ldcg(partials + cta0 + b);
   block_sum<1>(t);
   if (threadIdx.x == 0) {
     tot = t[0];
@@ -97,52 +100,62 @@ __device__ __forceinline__ bool slot_reduce(double v, const SlotDesc &D, int pha
   return true;
 }
 
+// One block row of the slot's sliced FP64 copy (slot t of slice sl): the
+// row sums of the single-solve product (sell_spmv_kernel), into y and (p, y).
 template <int B>
-__device__ __forceinline__ double row_product(const SlotDesc &D, int row) {
-  constexpr int BB = B * B;
-  const int I = row / B, a = row - I * B;
-  const int pb = D.bia[I], pe = D.bia[I + 1];
-  const double *vr = D.bval + (size_t)pb * BB + a * B;
-  double acc0 = 0.0, acc1 = 0.0;
-  int p = pb;
-  for (; p + 2 <= pe; p += 2) {
-    const int J0 = D.bja[p], J1 = D.bja[p + 1];
-    double v0[B], v1[B], x0[B], x1[B];
+__device__ __forceinline__ double slice_rows(const SlotDesc &D, int sl, int t) {
+  constexpr int BB = B * B, R = kSliceRows, Q = BB / 2;
+  const int g0 = D.sell_ptr[sl], g1 = D.sell_ptr[sl + 1];
+  double acc[B];
 #pragma unroll
-    for (int b = 0; b < B; b++) {
-      v0[b] = vr[(size_t)(p - pb) * BB + b];
-      v1[b] = vr[(size_t)(p + 1 - pb) * BB + b];
-      x0[b] = D.p[J0 * B + b];
-      x1[b] = D.p[J1 * B + b];
+  for (int a = 0; a < B; a++) acc[a] = 0.0;
+  for (int g = g0; g < g1; g++) {
+    const int J = D.sell_col[(size_t)g * R + t];
+    const double *grp = D.sval + (size_t)g * BB * R;
+    double bv[BB];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+      const double2 c = __ldg(reinterpret_cast<const double2 *>(grp + q * 2 * R + 2 * t));
+      bv[2 * q] = c.x;
+      bv[2 * q + 1] = c.y;
     }
 #pragma unroll
-    for (int b = 0; b < B; b++) {
-      acc0 += v0[b] * x0[b];
-      acc1 += v1[b] * x1[b];
+    for (int e = 2 * Q; e < BB; e++) bv[e] = __ldg(grp + 2 * Q * R + (e - 2 * Q) * R + t);
+    double xv[B];
+#pragma unroll
+    for (int b = 0; b < B; b++) xv[b] = D.p[J * B + b];
+#pragma unroll
+    for (int a = 0; a < B; a++)
+#pragma unroll
+      for (int b = 0; b < B; b++) acc[a] += bv[a * B + b] * xv[b];
+  }
+  const int I = sl * R + t;
+  double v = 0.0;
+  if (I < D.nb) {
+#pragma unroll
+    for (int a = 0; a < B; a++) {
+      const int row = I * B + a;
+      D.q[row] = acc[a];
+      v += D.p[row] * acc[a];
     }
   }
-  if (p < pe) {
-    const int J = D.bja[p];
-#pragma unroll
-    for (int b = 0; b < B; b++) acc0 += vr[(size_t)(p - pb) * BB + b] * D.p[J * B + b];
-  }
-  return acc0 + acc1;
+  return v;
 }
 
 // q = K p and (p, q) for every slot; alpha = d / (p, q)   (Iters.f:366-372)
+// One warp per slice of the slot's sliced copy, 8 slices per block.
 __global__ void __launch_bounds__(kThreads)
 packed_spmv_kernel(const SlotDesc *desc, int nslots, double *partials) {
-  const SlotDesc D = desc[find_slot(desc, nslots, blockIdx.x)];
+  const SlotDesc D = desc[find_slot<true>(desc, nslots, blockIdx.x)];
   if (D.sc->done) return;
-  const int row = (blockIdx.x - D.cta0) * kRowsPerCta + threadIdx.x;
+  const int sl = (blockIdx.x - D.scta0) * (kThreads / kSliceRows) + threadIdx.x / kSliceRows;
+  const int nsl = (D.nb + kSliceRows - 1) / kSliceRows;
   double v = 0.0;
-  if (row < D.n) {
-    const double y = D.bsize == 3 ? row_product<3>(D, row) : row_product<2>(D, row);
-    D.q[row] = y;
-    v = D.p[row] * y;
-  }
+  if (sl < nsl)
+    v = D.bsize == 3 ? slice_rows<3>(D, sl, threadIdx.x % kSliceRows)
+                     : slice_rows<2>(D, sl, threadIdx.x % kSliceRows);
   double tot;
-  if (!slot_reduce(v, D, 0, partials, tot)) return;
+  if (!slot_reduce(v, D, D.scta0, D.sncta, 0, partials, tot)) return;
   if (threadIdx.x == 0) {
     D.sc->pq = tot;
     D.sc->alpha = D.sc->d / tot;
@@ -153,7 +166,7 @@ packed_spmv_kernel(const SlotDesc *desc, int nslots, double *partials) {
 // test sqrt|d'| < tol ||b||_M                               (Iters.f:377-419)
 __global__ void __launch_bounds__(kThreads)
 packed_update_kernel(const SlotDesc *desc, int nslots, double *partials) {
-  const SlotDesc D = desc[find_slot(desc, nslots, blockIdx.x)];
+  const SlotDesc D = desc[find_slot<false>(desc, nslots, blockIdx.x)];
   if (D.sc->done) return;
   const int row = (blockIdx.x - D.cta0) * kRowsPerCta + threadIdx.x;
   double v = 0.0;
@@ -165,7 +178,7 @@ packed_update_kernel(const SlotDesc *desc, int nslots, double *partials) {
     v = ri * (ri * D.m[row]);
   }
   double tot;
-  if (!slot_reduce(v, D, 1, partials, tot)) return;
+  if (!slot_reduce(v, D, D.cta0, D.ncta, 1, partials, tot)) return;
   if (threadIdx.x == 0) {
     SlotScalars &S = *D.sc;
     S.iters += 1;
@@ -183,7 +196,7 @@ packed_update_kernel(const SlotDesc *desc, int nslots, double *partials) {
 // p = M r + beta p                                          (Iters.f:411-414)
 __global__ void __launch_bounds__(kThreads)
 packed_direction_kernel(const SlotDesc *desc, int nslots) {
-  const SlotDesc D = desc[find_slot(desc, nslots, blockIdx.x)];
+  const SlotDesc D = desc[find_slot<false>(desc, nslots, blockIdx.x)];
   if (D.sc->done) return;
   const int row = (blockIdx.x - D.cta0) * kRowsPerCta + threadIdx.x;
   if (row < D.n) D.p[row] = D.r[row] * D.m[row] + D.sc->beta * D.p[row];
@@ -334,6 +347,9 @@ int64_t estimate_bytes(const SrvRequest &q) {
     b += 8 * 2 * 16 * 1216 + (64 << 10);
   } else {
     b += 5 * 8 * n * q.nrhs;                           // per load case
+    // the sliced FP64 copy of the packed product: values, columns, pointers
+    const int64_t slots = (int64_t)s.sell_ptr[s.nslices] * elx::kSliceRows;
+    b += 8 * slots * s.bsize * s.bsize + 4 * slots + 4 * (s.nslices + 1) + 3 * 64;
   }
   b += 160 << 10;                                      // scalars, partials, padding
   return b;
@@ -448,6 +464,11 @@ void admit(elx_server *sv, SrvRequest &q) {
   assemble_resident(c);  // u = 0, b0 = 0: K only (the loads are the slots' b)
   build_preconditioner(c);
   const size_t n = (size_t)c->s.neq;
+  if (!q.large) {
+    // the packed product reads the sliced FP64 copy
+    ensure_sell64(c);
+    require(c->sell_val64.p != nullptr, ELX_ERR_STATE, "the sliced FP64 copy is switched off");
+  }
   if (q.large) {
     // b and x of all load cases (column-major) for the request's block solve
     c->alloc(q.vecs, 2 * n * q.nrhs * 8);
@@ -655,7 +676,7 @@ void large_loop(elx_server *sv) {
 void gpu_loop(elx_server *sv) {
   try {
     ELX_CUDA(cudaSetDevice(sv->device));
-    int nslots = 0, grid = 0;
+    int nslots = 0, grid = 0, sgrid = 0;
     bool repack = false;
     for (;;) {
       // 1. admitted requests join the pack
@@ -674,15 +695,21 @@ void gpu_loop(elx_server *sv) {
       if (repack) {
         nslots = 0;
         grid = 0;
+        sgrid = 0;
         for (auto &q : sv->active) {
           elx_ctx *c = q->ctx;
           const size_t n = (size_t)c->s.neq;
           double *base = q->vecs.as<double>() + n * q->nrhs;
+          const int per_cta = elx::kThreads / elx::kSliceRows;
           for (int k = 0; k < q->nrhs; k++) {
             SlotDesc &d = sv->h_desc[nslots++];
-            d.bia = c->bia.as<int32_t>();
-            d.bja = c->bja.as<int32_t>();
-            d.bval = c->bval.as<double>();
+            d.sell_ptr = c->sell_ptr.as<int32_t>();
+            d.sell_col = c->sell_col.as<int32_t>();
+            d.sval = c->sell_val64.as<double>();
+            d.nb = c->s.nb;
+            d.scta0 = sgrid;
+            d.sncta = (c->s.nslices + per_cta - 1) / per_cta;
+            sgrid += d.sncta;
             d.m = c->m.as<double>();
             d.x = base + (size_t)k * 4 * n;
             d.r = d.x + n;
@@ -697,12 +724,13 @@ void gpu_loop(elx_server *sv) {
           }
         }
         sv->peak_slots = std::max<int64_t>(sv->peak_slots.load(), nslots);
-        if ((size_t)grid * 8 > sv->part_bytes) {
+        const int pgrid = std::max(grid, sgrid);
+        if ((size_t)pgrid * 8 > sv->part_bytes) {
           if (sv->d_part) cudaFree(sv->d_part);
           sv->d_part = nullptr;
           sv->part_bytes = 0;
-          ELX_CUDA(cudaMalloc(&sv->d_part, (size_t)grid * 8 * 2));
-          sv->part_bytes = (size_t)grid * 8 * 2;
+          ELX_CUDA(cudaMalloc(&sv->d_part, (size_t)pgrid * 8 * 2));
+          sv->part_bytes = (size_t)pgrid * 8 * 2;
         }
         ELX_CUDA(cudaMemcpyAsync(sv->d_desc, sv->h_desc, nslots * sizeof(SlotDesc),
                                  cudaMemcpyHostToDevice, sv->stream));
@@ -712,7 +740,7 @@ void gpu_loop(elx_server *sv) {
       const SlotDesc *dd = static_cast<const SlotDesc *>(sv->d_desc);
       double *part = static_cast<double *>(sv->d_part);
       for (int it = 0; it < sv->poll_steps; it++) {
-        elx::packed_spmv_kernel<<<grid, elx::kThreads, 0, sv->stream>>>(dd, nslots, part);
+        elx::packed_spmv_kernel<<<sgrid, elx::kThreads, 0, sv->stream>>>(dd, nslots, part);
         elx::packed_update_kernel<<<grid, elx::kThreads, 0, sv->stream>>>(dd, nslots, part);
         elx::packed_direction_kernel<<<grid, elx::kThreads, 0, sv->stream>>>(dd, nslots);
       }
