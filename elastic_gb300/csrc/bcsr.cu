@@ -159,7 +159,7 @@ bcsr_spmv_kernel(int neq, const int32_t *__restrict__ bia, const int32_t *__rest
   if (threadIdx.x == 0) {
     if (EPI == kEpiPcg) {
       sc->pq = tot[0];
-      sc->alpha = sc->d / tot[0];
+      sc->alpha = tot[0] != 0.0 ? sc->d / tot[0] : 0.0;  // p = 0: no step
     } else if (EPI == kEpiBicgAlpha) {
       sc->pq = tot[0];
       sc->alpha = sc->rho / tot[0];
@@ -264,7 +264,7 @@ bcsr_spmv_group_kernel(int nb, const int32_t *__restrict__ bia, const int32_t *_
   if (threadIdx.x == 0) {
     if (EPI == kEpiPcg) {
       sc->pq = tot[0];
-      sc->alpha = sc->d / tot[0];
+      sc->alpha = tot[0] != 0.0 ? sc->d / tot[0] : 0.0;  // p = 0: no step
     } else if (EPI == kEpiBicgAlpha) {
       sc->pq = tot[0];
       sc->alpha = sc->rho / tot[0];
@@ -421,7 +421,7 @@ sell_spmv_kernel(int nb, int nslices, const int32_t *__restrict__ sell_ptr,
   if (threadIdx.x == 0) {
     if (EPI == kEpiPcg) {
       sc->pq = tot[0];
-      sc->alpha = sc->d / tot[0];
+      sc->alpha = tot[0] != 0.0 ? sc->d / tot[0] : 0.0;  // p = 0: no step
     } else if (EPI == kEpiBicgAlpha) {
       sc->pq = tot[0];
       sc->alpha = sc->rho / tot[0];

@@ -324,7 +324,7 @@ spmm_kernel(int nb, const int32_t *__restrict__ bia, const int32_t *__restrict__
       ColScalars &s = cols[threadIdx.x];
       if (!s.done) {
         s.pq = tot;
-        s.alpha = s.d / tot;
+        s.alpha = tot != 0.0 ? s.d / tot : 0.0;  // p = 0: no step
       }
     }
   }
@@ -398,7 +398,7 @@ bpcg_update_kernel(int n, const double *__restrict__ p, const double *__restrict
     ColScalars &s = cols[threadIdx.x];
     if (!s.done) {
       s.iters += 1;
-      s.beta = tot / s.d;
+      s.beta = s.d != 0.0 ? tot / s.d : 0.0;
       s.d = tot;
       if (sqrt(fabs(tot)) < s.conv) {
         s.done = 1;
@@ -529,15 +529,17 @@ brel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__
     ColScalars &s = cols[threadIdx.x];
     if (!s.done) {
       s.iters += 1;
-      if (!(tot == tot)) {
+      if (!(tot == tot) || isinf(tot)) {
+        // the FP32 recurrence broke down: this column is solved in FP64
         s.done = 1;
         s.status = ELX_ERR_NO_CONVERGENCE;
+        s.failed = 1;
       } else {
         const double rn = sqrt(fabs(tot));
-        s.beta = tot / s.d;
+        s.beta = s.d != 0.0 ? tot / s.d : 0.0;
         s.d = tot;
         if (rn < hdr->delta * s.rmax || rn < s.conv || s.iters >= hdr->maxit ||
-            s.iters - s.last_rep >= kMixedCheckEvery) {
+            s.iters - s.last_rep >= kMixedCheckEvery || rn > kMixedDiverge * s.rmax) {
           s.update = 1;
           hdr->any_update = 1;
         }

@@ -110,7 +110,7 @@ halo_dot_kernel(int neq, const int32_t *__restrict__ halo_ptr,
   gather_partials<1>(tot, partials, counter);
   if (threadIdx.x == 0) {
     sc->pq = tot[0];
-    sc->alpha = sc->d / tot[0];
+    sc->alpha = tot[0] != 0.0 ? sc->d / tot[0] : 0.0;  // p = 0: no step
   }
 }
 
@@ -333,15 +333,21 @@ rel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__ 
     const int it = sc->iters + 1;
     sc->iters = it;
     const double rn = sqrt(fabs(di));
-    if (!(di == di)) {
+    if (!(di == di) || isinf(di)) {
+      // the FP32 recurrence broke down (overflow): solve in FP64 instead
       sc->done = 1;
       sc->status = ELX_ERR_NO_CONVERGENCE;
+      sc->failed = 1;
       return;
     }
-    sc->beta = di / sc->d;
+    // an FP32 residual of exactly zero (a small system solved in FP32):
+    // beta = 0, and the next replacement point takes over
+    sc->beta = sc->d != 0.0 ? di / sc->d : 0.0;
     sc->d = di;
+    // a residual growing past kMixedDiverge x the last replaced one asks for
+    // a replacement too (whose progress watch then judges it)
     if (rn < sc->delta * sc->rmax || rn < sc->conv || it >= sc->maxit ||
-        it - sc->last_rep >= kMixedCheckEvery)
+        it - sc->last_rep >= kMixedCheckEvery || rn > kMixedDiverge * sc->rmax)
       sc->update = 1;
   }
 }

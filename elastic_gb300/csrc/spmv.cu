@@ -334,7 +334,7 @@ gather_spmv_kernel(int neq, const int32_t *__restrict__ ia, const int32_t *__res
   if (threadIdx.x == 0) {
     if (EPI == kEpiPcg) {
       sc->pq = tot[0];
-      sc->alpha = sc->d / tot[0];
+      sc->alpha = tot[0] != 0.0 ? sc->d / tot[0] : 0.0;  // p = 0: no step
     } else if (EPI == kEpiBicgAlpha) {
       sc->pq = tot[0];
       sc->alpha = sc->rho / tot[0];
