@@ -280,6 +280,20 @@ int elx_set_matrix(elx_ctx *ctx, const double *ad, const double *al);
  * elx_stream(ctx) and return once enqueued, except elx_solve_resident which
  * waits for convergence. */
 int elx_set_state(elx_ctx *ctx, const double *u, const double *b0);
+int elx_assemble_resident(elx_ctx *ctx);
+int elx_solve_resident(elx_ctx *ctx, int32_t solver, int32_t precision,
+                       double tol, int32_t maxit, int32_t ngram,
+                       elx_info *info);
+int elx_spmv_resident(elx_ctx *ctx, int32_t precision, int32_t reps);
+/* update_mec (Predict.f:183-209) on the resident state: u(j,i) =
+ * x(id(j,i)) for the free dofs, from the resident solution; with it a
+ * solvm pass (assemble, solve, update) and the stresses (elx_stress with
+ * u = NULL) never leave the device.  Stream-ordered like the calls above. */
+int elx_update_resident(elx_ctx *ctx);
+int elx_get_solution(elx_ctx *ctx, double *x);
+int elx_get_rhs(elx_ctx *ctx, double *b);
+
+/* ---- the steps around the solve -------------------------------------- */
 /* The load step on the device (replaces the host's pload_mec, Pload.f:2-58,
  * and pform_mec with isw = 4, Pform.f:1-11 / Elmlib02.f:260-314, 856-910):
  * f(ndf,nnode) evaluated nodal loads -> b0(id) = f for free dofs, u = f for
@@ -329,18 +343,6 @@ int elx_partition_info(elx_ctx *ctx, int32_t nparts, int32_t part, int32_t *eq0,
 /* Test hook of the device number formatter: n fields Ew.d (e = 0) or
  * Ew.dEe of x into out (n * w chars), as the writer prints them. */
 int elx_fortran_e(const double *x, int32_t n, int32_t w, int32_t d, int32_t e, char *out);
-int elx_assemble_resident(elx_ctx *ctx);
-int elx_solve_resident(elx_ctx *ctx, int32_t solver, int32_t precision,
-                       double tol, int32_t maxit, int32_t ngram,
-                       elx_info *info);
-int elx_spmv_resident(elx_ctx *ctx, int32_t precision, int32_t reps);
-/* update_mec (Predict.f:183-209) on the resident state: u(j,i) =
- * x(id(j,i)) for the free dofs, from the resident solution; with it a
- * solvm pass (assemble, solve, update) and the stresses (elx_stress with
- * u = NULL) never leave the device.  Stream-ordered like the calls above. */
-int elx_update_resident(elx_ctx *ctx);
-int elx_get_solution(elx_ctx *ctx, double *x);
-int elx_get_rhs(elx_ctx *ctx, double *b);
 
 /* ---- allocation-free SpMV + dot ---------------------------------------- */
 /* No counterpart in the reference: this entry point is for callers that
