@@ -352,12 +352,15 @@ __device__ __forceinline__ void sell_load(const T *grp, int t, T (&bv)[B * B]) {
 // any of their x gathers and FMAs.  Every lane of a warp runs the same number
 // of groups (the slice's width), so the FP64 form has no idle FMA lanes but
 // the padding.  Padding slots (zero values, the row's own column) do no harm.
-template <class T, int B, int U, bool LD, int EPI>
+// With D16 the column of slot (g, t) is its block row plus a 16-bit offset
+// (col16: half the index bytes), else sell_col's 32-bit column.
+template <class T, int B, int U, bool LD, int EPI, bool D16 = false>
 __global__ void __launch_bounds__(256)
 sell_spmv_kernel(int nb, int nslices, const int32_t *__restrict__ sell_ptr,
                  const int32_t *__restrict__ sell_col, const T *__restrict__ sval,
                  const T *__restrict__ x, T *__restrict__ y, const T *__restrict__ w,
-                 PcgScalars *sc, double *partials, unsigned int *counter, const int32_t *gate) {
+                 PcgScalars *sc, double *partials, unsigned int *counter, const int32_t *gate,
+                 const int16_t *__restrict__ col16 = nullptr) {
   constexpr bool DOT = EPI == kEpiPcg || EPI == kEpiBicgAlpha || EPI == kEpiBicgOmega;
   constexpr int NV = EPI == kEpiBicgOmega ? 2 : 1;
   constexpr int BB = B * B, R = kSliceRows;
@@ -379,7 +382,12 @@ sell_spmv_kernel(int nb, int nslices, const int32_t *__restrict__ sell_ptr,
       T bv[U][BB], xv[U][B];
 #pragma unroll
       for (int u = 0; u < U; u++)
-        if (u < nu) J[u] = sell_ld<LD>(sell_col + (size_t)(g + u) * R + t);
+        if (u < nu) {
+          if constexpr (D16)
+            J[u] = sl * R + t + (int)sell_ld<LD>(col16 + (size_t)(g + u) * R + t);
+          else
+            J[u] = sell_ld<LD>(sell_col + (size_t)(g + u) * R + t);
+        }
 #pragma unroll
       for (int u = 0; u < U; u++)
         if (u < nu) sell_load<T, B, LD>(sval + (size_t)(g + u) * BB * R, t, bv[u]);
@@ -512,7 +520,16 @@ void launch_bcsr(const CsrcDev &k, const T *x, T *y, const T *w, PcgScalars *sc,
       // one CTA per 8 slices, at most 8 per SM; 3 groups per step for B = 3
       // (64 registers) and 4 for B = 2: 50.7 / 52.4 / 50.2 / 60.0 us for
       // 1 / 2 / 3 / 4 groups with streaming loads on the 64^3 HEXA8 cube
-      if (k.bsize == 3) {
+#define ELX_SELL16(B_, U_, LD_)                                                          \
+  sell_spmv_kernel<float, B_, U_, LD_, EPI, true><<<sgrid, 256, 0, st>>>(                  \
+      k.nb, k.nslices, k.sell_ptr, k.sell_col, k.sell_val, x, y, w, sc, partials, counter, \
+      gate, k.sell_d16)
+      if (k.bsize == 3 && k.sell_d16) {
+        if (k.sell_stream)
+          ELX_SELL16(3, 3, true);
+        else
+          ELX_SELL16(3, 3, false);
+      } else if (k.bsize == 3) {
         if (k.sell_stream)
           ELX_SELL(float, 3, 3, true, k.sell_val);
         else
@@ -523,6 +540,7 @@ void launch_bcsr(const CsrcDev &k, const T *x, T *y, const T *w, PcgScalars *sc,
         else
           ELX_SELL(float, 2, 4, false, k.sell_val);
       }
+#undef ELX_SELL16
       ELX_CUDA(cudaGetLastError());
       return;
     }

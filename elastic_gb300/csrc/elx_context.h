@@ -37,7 +37,7 @@ struct elx_ctx {
   // streaming loads unless it fits in 60 % of L2 (ELX_SELL_STREAM=0/1 forces
   // either: 49.7 against 54.5 us on the 64^3 HEXA8 cube, 277 MB; 17.2
   // against 12.6 us on the 48^3 TETRA4 mesh, 64 MB)
-  DBuf sell_ptr, sell_col, sell_val, sell_val64;
+  DBuf sell_ptr, sell_col, sell_val, sell_val64, sell_d16;
   bool sell_stream = true;
   bool use_blocks = false;
   // tiled transposed index of the SpMV and its halo slots
@@ -175,6 +175,7 @@ struct elx_ctx {
       k.sell_val = sell_val.as<float>();
       k.sell_stream = sell_stream;
       k.sell_val64 = sell_val64.as<double>();
+      k.sell_d16 = static_cast<const int16_t *>(sell_d16.p);
     }
     return k;
   }

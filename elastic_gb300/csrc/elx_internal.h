@@ -192,6 +192,9 @@ struct CsrcDev {
   float *sell_val = nullptr;
   bool sell_stream = true;  // streaming loads (the copy does not stay in L2)
   double *sell_val64 = nullptr;  // sliced FP64 copy (null: the FP64 product reads bval)
+  // the FP32 product's columns as 16-bit offsets from the block row (null:
+  // the matrix's block bandwidth does not fit; sell_col is read)
+  const int16_t *sell_d16 = nullptr;
 };
 
 struct TileDev {

@@ -124,6 +124,12 @@ __device__ __forceinline__ float ld_stream(const float *p) {
   return v;
 }
 
+__device__ __forceinline__ int16_t ld_stream(const int16_t *p) {
+  int16_t v;
+  asm volatile("ld.global.nc.L1::no_allocate.s16 %0, [%1];" : "=h"(v) : "l"(p));
+  return v;
+}
+
 __device__ __forceinline__ int32_t ld_stream(const int32_t *p) {
   int32_t v;
   asm volatile("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
