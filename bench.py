@@ -94,7 +94,10 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{gpu}.csv")
+        # the raw samples (ELX_CLOCKS_DIR, else the system's temporary folder)
+        import tempfile
+        folder = os.environ.get("ELX_CLOCKS_DIR", tempfile.gettempdir())
+        self.path = os.path.join(folder, f"elx_clocks_bench_{gpu}.csv")
 
     def start(self):
         try:

@@ -347,7 +347,7 @@ rel_update_kernel(int n, const float *__restrict__ p, const float *__restrict__ 
     sc->beta = sc->d != 0.0 ? di / sc->d : 0.0;
     sc->d = di;
     // a residual growing past kMixedDiverge x the last replaced one asks for
-    // a replacement too (whose progress watch then judges it)
+    // a replacement too (whose progress watch then weighs it)
     if (rn < sc->delta * sc->rmax || rn < sc->conv || it >= sc->maxit ||
         it - sc->last_rep >= kMixedCheckEvery || rn > kMixedDiverge * sc->rmax)
       sc->update = 1;
