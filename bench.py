@@ -601,9 +601,21 @@ def cpu_baseline(mesh, st, b0, u0, full_iters=None, sample_iters=300, nthreads=N
         sample = (f"full OpenMP assembly + {info['iters']} PCG iterations, scaled to "
                   f"{full_iters} iterations")
     total = t_asm + t_pcg
+    # the sequential path (pform_mec's element loop, matvec_csrcsym1 and pcg
+    # on one thread): one full assembly and a 30-iteration sample
+    t = time.perf_counter()
+    O.assemble(mesh, s, u0, b0)
+    t_asm1 = time.perf_counter() - t
+    n1 = min(30, full_iters)
+    _, info1 = O.pcg(s, ad, al, b, tol=TOL, maxit=n1)
+    t_pcg1 = info1["seconds"] * full_iters / max(info1["iters"], 1)
     return {"value": 1.0 / total, "unit": "solves/s", "cores": nth, "kind": "port",
             "sample": sample, "seconds_per_solve": total, "assembly_s": t_asm,
-            "pcg_s": t_pcg}
+            "pcg_s": t_pcg,
+            "sequential_1thread": {"value": 1.0 / (t_asm1 + t_pcg1), "unit": "solves/s",
+                                   "cores": 1, "assembly_s": t_asm1, "pcg_s": t_pcg1,
+                                   "sample": f"full assembly + {info1['iters']} PCG "
+                                             f"iterations, scaled to {full_iters}"}}
 
 
 def run_reference(args, dist: Dist):
