@@ -13,8 +13,10 @@ b in, x out) copied every step.  Sub-objects: `mixed` (the same step with
 the mixed-precision solver), `after_solve` (the device load step, stress
 recovery and the result file on the solution, against the oracle's stress
 recovery and writer; the product through 4 row-block partitions), `block`
-(16 load cases of the 96x96x48 plate) and `serve` (a served request stream
-against sequential plain FP64 solves).
+(16 load cases of the 96x96x48 plate), `tetra` (FP64 and mixed PCG to 1e-10
+on the 48^3 TETRA4 mesh with per-element materials, against the oracle's
+FP64 solve) and `serve` (a served request stream against sequential plain
+FP64 solves).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -476,6 +478,65 @@ def run_block(args):
             "rel_err_vs_fp64_case0": err}
 
 
+def run_tetra(args):
+    """The TETRA4 mesh of a 48^3 cube (6 tetrahedra per hex, interior nodes
+    jittered, one lognormal E and uniform nu per element: 345,744 equations),
+    z=0 fixed, unit pressure on z=1, tol 1e-10: FP64 PCG and the mixed-
+    precision solver on the device (assembly excluded, CUDA events), each
+    solution against the oracle's FP64 pcg_omp solve on this host's cores
+    (timed: the CPU baseline of this mesh)."""
+    import torch
+
+    import elastic_gb300 as E
+    import oracle as O
+    from elastic_gb300 import meshgen as M
+
+    tol = 1e-10
+    mesh = M.cube_tetra4_48_mixed()
+    ctx = E.Context(device=0)
+    ctx.set_mesh(mesh)
+    neq, nad, _ = ctx.build_structure(True)
+    st = ctx.structure()
+    b0, u0 = E.pload(mesh, st.id)
+    ctx.set_state(u0, b0)
+    ctx.assemble_resident()
+    ext = torch.cuda.ExternalStream(ctx.stream, device=0)
+
+    def timed(prec):
+        ms, info = [], None
+        for k in range(args.warmup + args.steps):
+            e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+            e0.record(ext)
+            info = ctx.solve_resident(precision=prec, tol=tol, maxit=MAXIT)
+            e1.record(ext)
+            torch.cuda.synchronize(0)
+            if k >= args.warmup:
+                ms.append(e0.elapsed_time(e1))
+        return statistics.median(ms), info, ctx.solution()
+
+    ms64, i64, x64 = timed(E.PREC_FP64)
+    msm, im, xm = timed(E.PREC_MIXED)
+    ctx.close()
+    # the oracle's FP64 solve on the same equations (numbering, ia/ja identical)
+    nth = len(os.sched_getaffinity(0))
+    s = O.Structure(perm=st.perm, id=st.id, neq=st.neq, nad=st.nad, ia=st.ia, ja=st.ja)
+    ad, al, b = O.assemble_omp(mesh, s, u0, b0, nthreads=nth)
+    xo, io = O.pcg_omp(s, ad, al, b, tol=tol, maxit=MAXIT, nthreads=nth)
+    rel = lambda a, ref: float(np.abs(a - ref).max() / np.abs(ref).max())
+    return {"mode": "tetra",
+            "workload": ("TETRA4 of a 48^3 cube (6 per hex), jittered interior nodes, lognormal E "
+                         "per element, z=0 fixed, unit pressure on z=1, RCM, tol 1e-10"),
+            "neq": neq, "nad": nad,
+            "fp64": {"pcg_ms": ms64, "iters": i64["iters"]},
+            "mixed": {"pcg_ms": msm, "inner_iters": im["iters"],
+                      "refinements": im["refinements"], "speedup_vs_fp64": ms64 / msm},
+            "rel_err_fp64_vs_oracle": rel(x64, xo), "rel_err_mixed_vs_oracle": rel(xm, xo),
+            "rel_err_mixed_vs_fp64": rel(xm, x64),
+            "cpu_baseline": {"value": 1.0 / io["seconds"], "unit": "solves/s (PCG only)",
+                             "cores": nth, "kind": "port", "iters": io["iters"],
+                             "sample": "the full pcg_omp solve (matvec_csrcsym_omp)"}}
+
+
 def run_serve(args):
     """The served stream: N requests (box meshes of the four element types,
     2k-2M dofs log-uniform, 1-8 load cases, tol 1e-8) with Poisson arrivals at
@@ -667,10 +728,12 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
-                    help="full mode: skip the block and serve sub-benchmarks")
-    ap.add_argument("--mode", choices=["full", "spmv", "block", "serve"], default="full",
+                    help="full mode: skip the block, tetra and serve sub-benchmarks")
+    ap.add_argument("--mode", choices=["full", "spmv", "block", "tetra", "serve"],
+                    default="full",
                     help="spmv: only the SpMV of the workload (for profiling); block: 16 load "
-                         "cases on the 96x96x48 plate; serve: the served request stream")
+                         "cases on the 96x96x48 plate; tetra: FP64 and mixed PCG on the "
+                         "48^3 TETRA4 mesh; serve: the served request stream")
     ap.add_argument("--requests", type=int, default=512, help="serve: requests in the stream")
     ap.add_argument("--max-dof", type=float, default=2e6, help="serve: largest request")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
@@ -685,17 +748,20 @@ def main():
             out = run_spmv_only(args)
         elif args.mode == "block":
             out = run_block(args)
+        elif args.mode == "tetra":
+            out = run_tetra(args)
         elif args.mode == "serve":
             out = run_serve(args)
         else:
             out = run_ours(args, dist)
             if out is not None and dist.ws == 1 and not args.no_extras:
-                # the other two headline workloads, at their own sizes (block) and
-                # on a shortened stream (serve: 64 requests up to 2e5 dofs; the
-                # full 512-request stream is --mode serve)
+                # the other headline workloads, at their own sizes (block, tetra)
+                # and on a shortened stream (serve: 64 requests up to 2e5 dofs;
+                # the full 512-request stream is --mode serve)
                 blk = argparse.Namespace(**vars(args))
                 blk.steps, blk.warmup = 3, 3
                 out["block"] = run_block(blk)
+                out["tetra"] = run_tetra(blk)
                 srv = argparse.Namespace(**vars(args))
                 srv.requests, srv.max_dof = 64, 2e5
                 out["serve"] = run_serve(srv)

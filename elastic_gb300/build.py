@@ -6,6 +6,7 @@ Usage: python -m elastic_gb300.build [--force]
 from __future__ import annotations
 
 import concurrent.futures as cf
+import fcntl
 import os
 import shutil
 import subprocess
@@ -40,7 +41,18 @@ def _stale(target, deps):
 
 
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
+    """Compiles the stale translation units and relinks the library.  Several
+    processes may call this at once (test workers): one builds under an
+    exclusive lock while the others wait, and every object and the library
+    are written to a temporary name and renamed into place, so that no
+    process maps a half-written library."""
     os.makedirs(OUT, exist_ok=True)
+    with open(os.path.join(OUT, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        return _build(force, verbose, ptxas_info)
+
+
+def _build(force: bool, verbose: bool, ptxas_info: bool) -> str:
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
     headers.append(os.path.join(ROOT, "include", "elastic_gb300.h"))
     nv = nvcc()
@@ -51,14 +63,17 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
         if force or ptxas_info or _stale(o, [s, *headers, __file__]):
             extra = ["-Xptxas", "-v"] if ptxas_info and src.endswith(".cu") else []
             if src.endswith(".cpp"):
-                cmd = [nv, "-x", "cu", *_flags(extra), "-c", s, "-o", o]
+                cmd = [nv, "-x", "cu", *_flags(extra), "-c", s, "-o", o + ".tmp"]
             else:
-                cmd = [nv, *_flags(extra), "-c", s, "-o", o]
-            jobs.append(cmd)
+                cmd = [nv, *_flags(extra), "-c", s, "-o", o + ".tmp"]
+            jobs.append((cmd, o))
     objs = [os.path.join(OUT, s + ".o") for s in SOURCES]
 
-    def run(cmd):
+    def run(job):
+        cmd, o = job
         r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode == 0:
+            os.replace(o + ".tmp", o)
         return cmd, r
 
     if jobs:
@@ -69,12 +84,13 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
                 if r.returncode != 0:
                     raise RuntimeError("nvcc failed: " + " ".join(cmd))
     if force or jobs or _stale(LIB, objs):
-        cmd = [nv, "-shared", *ARCH, "-o", LIB, *objs, "-lcudart_static", "-lrt", "-ldl",
-               "-lpthread"]
+        cmd = [nv, "-shared", *ARCH, "-o", LIB + ".tmp", *objs, "-lcudart_static", "-lrt",
+               "-ldl", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
             raise RuntimeError("link failed: " + " ".join(cmd))
+        os.replace(LIB + ".tmp", LIB)
     return LIB
 
 

@@ -13,6 +13,7 @@ wrapper that also replays the reference driver's ``solvm`` sequence
 from __future__ import annotations
 
 import ctypes as C
+import fcntl
 import os
 import subprocess
 from dataclasses import dataclass
@@ -47,8 +48,13 @@ class Info(C.Structure):
 
 
 def build():
-    """Compile oracle/_build/liboracle.so with the committed Makefile."""
-    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    """Compile oracle/_build/liboracle.so with the committed Makefile (under
+    an exclusive lock: test workers may ask at once; the Makefile links to a
+    temporary name and renames it into place)."""
+    os.makedirs(os.path.join(_HERE, "_build"), exist_ok=True)
+    with open(os.path.join(_HERE, "_build", ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
 
 
 def lib():
