@@ -444,6 +444,19 @@ void spmv64(elx_ctx *c, const double *x, double *y) {
   c->launches += c->spmv_kind == elx::kSpmvTiled ? 2 : 1;
 }
 
+// A bounded device wait of the pipelined (tiled) SpMV that gave up leaves
+// its code in flags[2]; reported, and cleared, as ELX_ERR_TIMEOUT.
+void check_pipe_waits(elx_ctx *c) {
+  ELX_CUDA(cudaMemcpyAsync(c->h_flags + 2, c->flags.as<int32_t>() + 2, sizeof(int32_t),
+                           cudaMemcpyDeviceToHost, c->stream));
+  c->sync();
+  if (c->h_flags[2] != 0) {
+    ELX_CUDA(cudaMemsetAsync(c->flags.as<int32_t>() + 2, 0, sizeof(int32_t), c->stream));
+    c->sync();
+    throw Error{ELX_ERR_TIMEOUT, "a bounded device wait of the SpMV pipeline gave up"};
+  }
+}
+
 // Post-solve diagnostics (Iters.f:433-458) of the resident x: z = K x,
 // xKx, ||x||, ||b - Kx||_M, ||b - Kx|| into h_diag[0..3].
 void post_diagnostics(elx_ctx *c) {
@@ -454,15 +467,7 @@ void post_diagnostics(elx_ctx *c) {
   c->launches += 1;
   ELX_CUDA(cudaMemcpyAsync(c->h_diag, c->diag.p, 4 * sizeof(double), cudaMemcpyDeviceToHost,
                            c->stream));
-  // a bounded device wait that gave up (pipelined SpMV) leaves its code here
-  ELX_CUDA(cudaMemcpyAsync(c->h_flags + 2, c->flags.as<int32_t>() + 2, sizeof(int32_t),
-                           cudaMemcpyDeviceToHost, c->stream));
-  c->sync();
-  if (c->h_flags[2] != 0) {
-    ELX_CUDA(cudaMemsetAsync(c->flags.as<int32_t>() + 2, 0, sizeof(int32_t), c->stream));
-    c->sync();
-    throw Error{ELX_ERR_TIMEOUT, "a bounded device wait of the SpMV pipeline gave up"};
-  }
+  check_pipe_waits(c);
 }
 
 void set_scalars(elx_ctx *c, double tol, int maxit) {
@@ -1641,6 +1646,7 @@ int elx_spmv(elx_ctx *c, int32_t precision, const double *x, double *y) {
     }
     ELX_CUDA(cudaMemcpyAsync(y, c->q.p, n * 8, cudaMemcpyDeviceToHost, c->stream));
     c->sync();
+    if (c->spmv_kind == elx::kSpmvTiled) check_pipe_waits(c);
   });
 }
 

@@ -59,12 +59,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Waits for the barrier phase `parity` with an iteration limit.  On timeout
-// it stores `code` into *err and returns false.
+// The GPU's nanosecond clock.
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Waits for the barrier phase `parity` for at most limit_ns nanoseconds (each
+// try_wait may itself suspend for a while, so the bound is on the clock, with
+// an iteration cap behind it).  On timeout it stores `code` into *err and
+// returns false.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, int32_t *err,
-                                                  int32_t code) {
-  for (uint32_t it = 0; it < (1u << 22); it++) {
+                                                  int32_t code,
+                                                  uint64_t limit_ns = 1000000000ull) {
+  const uint64_t t0 = global_ns();
+  for (uint32_t it = 0; it < (1u << 24); it++) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > limit_ns) break;
     if (it > 64) __nanosleep(64);
   }
   atomicExch(err, code);

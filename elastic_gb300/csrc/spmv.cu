@@ -84,7 +84,8 @@ template <class T>
 __global__ void __launch_bounds__(kPipeThreads, 2)
 spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32_t *__restrict__ ja,
                  const int32_t *__restrict__ ia, TileDev td, PipeLayout L,
-                 const T *__restrict__ x, T *__restrict__ y, T *__restrict__ part, int32_t *err) {
+                 const T *__restrict__ x, T *__restrict__ y, T *__restrict__ part, int32_t *err,
+                 int stall) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int PV = 16 / sizeof(T);  // elements per 16 bytes
   const int tid = threadIdx.x;
@@ -139,13 +140,15 @@ spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32
     if (c1 > c0) ptx::bulk_g2s(st + L.tcol, td.tgt_col + c0, (c1 - c0) * 4, &bar[s]);
   };
 
-  // ---- one tile ahead: gathers of x(ja), own x and ad; entry -> row map
-  auto gather = [&](int i) {
+  // ---- one tile ahead: gathers of x(ja), own x and ad; entry -> row map.
+  // False when the tile's copies did not arrive within the wait's limit
+  // (err is set): nothing of the tile is read then.
+  auto gather = [&](int i) -> bool {
     const int s = i % kStages;
     unsigned char *st = stages + (size_t)s * L.bytes;
     const int32_t *d = sdesc + 8 * s;
+    if (!ptx::mbar_wait_bounded(&bar[s], (uint32_t)((i / kStages) & 1), err, 1)) return false;
     const int base = d[0], nnz = d[1], r0 = d[6], nr = d[7];
-    ptx::mbar_wait_bounded(&bar[s], (uint32_t)((i / kStages) & 1), err, 1);
     const int32_t *s_ja = reinterpret_cast<const int32_t *>(st + L.ja) + (base & 3);
     const int32_t *s_ia = reinterpret_cast<const int32_t *>(st + L.ia) + (r0 & 3);
     T *s_xj = reinterpret_cast<T *>(st + L.xj);
@@ -159,9 +162,12 @@ spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32
       const int kb = s_ia[r] - base, ke = s_ia[r + 1] - base;
       for (int k = kb; k < ke; k++) s_row[k] = (uint8_t)r;
     }
+    return true;
   };
 
-  if (tid == 0) {
+  // stall != 0 (a test of the bounded waits): the producer issues nothing,
+  // so that every wait runs out
+  if (tid == 0 && !stall) {
     for (int i = 0; i < kStages - 1 && i < my_n; i++) {
       load_desc(i);
       issue(i);
@@ -169,18 +175,29 @@ spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32
     if (kStages - 1 < my_n) load_desc(kStages - 1);
   }
   __syncthreads();
-  gather(0);
+  bool ok = gather(0);
   ptx::cp_async_commit();
 
   for (int i = 0; i < my_n; i++) {
-    if (tid == 0 && i + kStages - 1 < my_n) {
+    if (tid == 0 && !stall && i + kStages - 1 < my_n) {
       issue(i + kStages - 1);
       if (i + kStages < my_n) load_desc(i + kStages);
     }
-    if (i + 1 < my_n) gather(i + 1);
+    if (ok && i + 1 < my_n) ok = gather(i + 1);
     ptx::cp_async_commit();
     ptx::cp_async_wait<1>();
-    __syncthreads();
+    if (__syncthreads_or(!ok)) {
+      // a wait ran out (err is set): no further tile is read or computed;
+      // the gathers already issued land, and thread 0 gives the bulk copies
+      // still in flight (tiles i .. i + kStages - 1) 10 ms each before the
+      // CTA leaves
+      ptx::cp_async_wait<0>();
+      if (tid == 0)
+        for (int j = i; j < my_n && j < i + kStages; j++)
+          ptx::mbar_wait_bounded(&bar[j % kStages], (uint32_t)((j / kStages) & 1), err, 1,
+                                 10000000ull);
+      return;
+    }
 
     // ---- compute tile i
     const int s = i % kStages;
@@ -401,8 +418,12 @@ void launch_tile(const CsrcDev &k, const TileDev &t, const T *al, const T *ad, c
   const size_t smem = pipe_header(t.rows, vs) + (size_t)kStages * L.bytes;
   // two CTAs per SM, so that one CTA's barriers overlap the other's arithmetic
   const int grid = std::min(t.ntiles, 2 * (g_num_sms > 0 ? g_num_sms : 148));
+  // ELX_PIPE_STALL_TEST=1: the waits run out on purpose (tests of the
+  // timeout path; read at every launch)
+  const char *env = getenv("ELX_PIPE_STALL_TEST");
+  const int stall = env && atoi(env) == 1 ? 1 : 0;
   spmv_pipe_kernel<T><<<grid, kPipeThreads, smem, st>>>(al, ad, k.ja, k.ia, t, L, x, ytile, part,
-                                                       err);
+                                                       err, stall);
   ELX_CUDA(cudaGetLastError());
 }
 
