@@ -214,8 +214,10 @@ struct PcgScalars;
 size_t tile_smem_bytes(const TileDev &t, bool fp32);
 size_t pipe_smem_bytes(int max_nnz, int max_tgt, int rows, bool fp32);
 void prepare_tile_kernels(const TileDev &t);
+// sc (nullable): the launch does nothing once the solve it belongs to is done
 void launch_tile_spmv64(const CsrcDev &k, const TileDev &t, const double *x, double *ytile,
-                        double *part, int32_t *err, cudaStream_t st);
+                        double *part, int32_t *err, cudaStream_t st,
+                        const PcgScalars *sc = nullptr);
 void launch_tile_spmv32(const CsrcDev &k, const TileDev &t, const float *x, float *ytile,
                         float *part, int32_t *err, cudaStream_t st);
 // Stress recovery (stress.cu): nodal stress sums of one colour segment, then

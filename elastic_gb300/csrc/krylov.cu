@@ -479,7 +479,7 @@ void launch_pcg_iteration(const CsrcDev &k, const TileDev &td, int spmv_kind, do
                           int32_t *err, cudaStream_t st) {
   const int n = k.neq;
   if (spmv_kind == kSpmvTiled) {
-    launch_tile_spmv64(k, td, p, q, part, err, st);
+    launch_tile_spmv64(k, td, p, q, part, err, st, sc);
     halo_dot_kernel<<<vector_grid(n), kThreads, 0, st>>>(n, td.halo_ptr, td.halo_slot, part, p,
                                                          q, sc, partials, counters + 0);
   } else {

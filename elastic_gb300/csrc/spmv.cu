@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kPipeThreads, 2)
 spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32_t *__restrict__ ja,
                  const int32_t *__restrict__ ia, TileDev td, PipeLayout L,
                  const T *__restrict__ x, T *__restrict__ y, T *__restrict__ part, int32_t *err,
-                 int stall) {
+                 int stall, const PcgScalars *sc) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int PV = 16 / sizeof(T);  // elements per 16 bytes
   const int tid = threadIdx.x;
@@ -98,6 +98,7 @@ spmv_pipe_kernel(const T *__restrict__ al, const T *__restrict__ ad, const int32
 
   const int ntiles = td.ntiles;
   if ((int)blockIdx.x >= ntiles) return;
+  if (sc && sc->done) return;  // an iteration past the solve's convergence
   const int my_n = (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;
 
   if (tid == 0) {
@@ -412,7 +413,7 @@ int g_num_sms = 0;
 
 template <class T>
 void launch_tile(const CsrcDev &k, const TileDev &t, const T *al, const T *ad, const T *x,
-                 T *ytile, T *part, int32_t *err, cudaStream_t st) {
+                 T *ytile, T *part, int32_t *err, const PcgScalars *sc, cudaStream_t st) {
   const int vs = sizeof(T);
   const PipeLayout L = pipe_layout(t.max_nnz, t.max_tgt, t.rows, vs);
   const size_t smem = pipe_header(t.rows, vs) + (size_t)kStages * L.bytes;
@@ -423,7 +424,7 @@ void launch_tile(const CsrcDev &k, const TileDev &t, const T *al, const T *ad, c
   const char *env = getenv("ELX_PIPE_STALL_TEST");
   const int stall = env && atoi(env) == 1 ? 1 : 0;
   spmv_pipe_kernel<T><<<grid, kPipeThreads, smem, st>>>(al, ad, k.ja, k.ia, t, L, x, ytile, part,
-                                                       err, stall);
+                                                       err, stall, sc);
   ELX_CUDA(cudaGetLastError());
 }
 
@@ -453,13 +454,13 @@ void prepare_tile_kernels(const TileDev &t) {
 }
 
 void launch_tile_spmv64(const CsrcDev &k, const TileDev &t, const double *x, double *ytile,
-                        double *part, int32_t *err, cudaStream_t st) {
-  launch_tile<double>(k, t, k.al, k.ad, x, ytile, part, err, st);
+                        double *part, int32_t *err, cudaStream_t st, const PcgScalars *sc) {
+  launch_tile<double>(k, t, k.al, k.ad, x, ytile, part, err, sc, st);
 }
 
 void launch_tile_spmv32(const CsrcDev &k, const TileDev &t, const float *x, float *ytile,
                         float *part, int32_t *err, cudaStream_t st) {
-  launch_tile<float>(k, t, k.al32, k.ad32, x, ytile, part, err, st);
+  launch_tile<float>(k, t, k.al32, k.ad32, x, ytile, part, err, nullptr, st);
 }
 
 // FP32 copies of ad, al and alt for the mixed-precision inner iteration.
