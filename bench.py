@@ -323,6 +323,20 @@ def run_ours(args, dist: Dist):
            "vtk_ms": 1e3 * statistics.median(vt_s), "vtk_bytes": vtk_bytes,
            "partitioned_spmv": part}
 
+    # the FP64 product's floor on this part: one DFMA per stored entry of the
+    # full matrix (2 nad + neq) at 2 DFMA per clock per SM (measured with a
+    # register-only FMA loop), at the SM clock sampled during the run
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
+    fp64_floor = None
+    if mhz:
+        dfma = 2 * nad + neq
+        floor_us = dfma / (2.0 * sms * mhz * 1e6) * 1e6
+        fp64_floor = {"dfma_per_launch": dfma, "dfma_per_clock_per_sm": 2, "sms": sms,
+                      "sm_mhz": mhz, "floor_us": floor_us,
+                      "floor_gbs": spmv_bytes / (floor_us * 1e-6) / 1e9,
+                      "frac_of_floor": floor_us / (spmv_ms * 1e3)}
+
     out = None
     if dist.rank == 0:
         n = dist.ws
@@ -344,7 +358,8 @@ def run_ours(args, dist: Dist):
                          "frac": spmv_gbs / peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": spmv_bytes,
                          "traffic": profiled("traffic_bytes_per_launch"),
-                         "fp64_pipe_frac_ncu": profiled("fp64_pipe_frac")},
+                         "fp64_pipe_frac_ncu": profiled("fp64_pipe_frac"),
+                         "fp64_floor": fp64_floor},
             "mixed": {"ms_per_step": mixed_step, "solves_per_s": n * 1000.0 / mixed_step,
                       "speedup_vs_fp64": ms_step / mixed_step,
                       "pcg_ms": statistics.median(mixed_pcg_ms),
