@@ -21,8 +21,9 @@ from dataclasses import dataclass
 import numpy as np
 
 __all__ = ["ElasticError", "Context", "Server", "Info", "load", "library_path", "pform_mec",
-           "solv", "pload", "edge_loads", "host_structure", "host_partition", "fortran_e",
-           "solvm", "SOLVER_PCG", "SOLVER_GMRES", "SOLVER_BICGSTAB", "PREC_FP64",
+           "solv", "pload", "edge_loads", "host_structure", "host_colors", "host_partition", "fp64_fma_rate",
+           "fortran_e",
+           "solvm", "SOLVER_PCG", "SOLVER_GMRES", "SOLVER_BICGSTAB", "SOLVER_BICGSTAB_NOPREC", "PREC_FP64",
            "PREC_MIXED", "VTK_VTU_ASCII", "VTK_LEGACY_BINARY", "VTK_DESLOC", "VTK_STRESS"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -30,7 +31,7 @@ _LIB_PATH = os.path.join(_HERE, "_build", "libelastic_gb300.so")
 
 OK, ERR_ZERO_DIAG, ERR_NO_CONVERGENCE, ERR_BAD_DET, ERR_OOM, ERR_TIMEOUT, ERR_ARG, \
     ERR_BAD_ELEMENT, ERR_CUDA, ERR_STATE = range(10)
-SOLVER_PCG, SOLVER_GMRES, SOLVER_BICGSTAB = 1, 2, 4
+SOLVER_PCG, SOLVER_GMRES, SOLVER_BICGSTAB, SOLVER_BICGSTAB_NOPREC = 1, 2, 4, 5
 PREC_FP64, PREC_MIXED = 0, 1
 VTK_VTU_ASCII, VTK_LEGACY_BINARY = 0, 1   # result file formats
 VTK_DESLOC, VTK_STRESS = 1, 2             # result fields (fprint(2), fprint(3))
@@ -128,6 +129,7 @@ def load():
                                                 _I32, C.c_int32]),
         "elx_host_structure_sizes": (C.c_int, [_VP, P(C.c_int32), P(C.c_int64)]),
         "elx_host_structure_get": (C.c_int, [_VP, _VP, _VP, _VP, _VP]),
+        "elx_host_structure_colors": (C.c_int, [_VP, _VP, _VP]),
         "elx_host_structure_destroy": (None, [_VP]),
         "elx_get_rhs": (C.c_int, [_VP, _F64]),
         "elx_spmv_dot_noalloc": (C.c_int, [C.c_int32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
@@ -150,6 +152,7 @@ def load():
         "elx_write_vtk": (C.c_int, [_VP, C.c_char_p, C.c_int32, C.c_int32, _VP]),
         "elx_format_vtk": (C.c_int, [_VP, C.c_int32, C.c_int32, _VP, C.c_int64, _VP]),
         "elx_fortran_e": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_int32, C.c_int32, _VP]),
+        "elx_fp64_fma_rate": (C.c_int, [C.c_int32, _VP, _VP]),
         "elx_get_state": (C.c_int, [_VP, _VP, _VP]),
         "elx_server_create": (C.c_int, [P(_VP), P(ServerOpts)]),
         "elx_server_destroy": (None, [_VP]),
@@ -213,6 +216,39 @@ def host_structure(mesh, reorder: bool = True) -> StructureArrays:
     finally:
         L.elx_host_structure_destroy(h)
     return StructureArrays(perm, idm, ia, ja[:nad], neq, nad, 0)
+
+
+def fp64_fma_rate(device: int = 0):
+    """(FP64 FMAs per second, per clock per SM at the maximum SM clock) of
+    the device, from the library's register-only probe kernel."""
+    L = load()
+    rate, per = C.c_double(), C.c_double()
+    st = L.elx_fp64_fma_rate(device, C.byref(rate), C.byref(per))
+    if st != OK:
+        raise ElasticError(st, "FP64 rate probe failed")
+    return rate.value, per.value
+
+
+def host_colors(mesh) -> np.ndarray:
+    """The element colours of the library's assembly (1-based, one per
+    element in element order): elx_host_structure_colors."""
+    L = load()
+    h = _VP()
+    st = L.elx_host_structure_create(C.byref(h), mesh.ndm, mesh.ndf, mesh.nen, mesh.numel,
+                                     mesh.nnode, _i32(mesh.ix), _i32(mesh.ie), mesh.numat,
+                                     _i32(mesh.id), 1)
+    if st != OK:
+        raise ElasticError(st, "host structure build failed")
+    try:
+        col = np.zeros(mesh.numel, np.int32)
+        nc = C.c_int32()
+        st = L.elx_host_structure_colors(h, _ptr(col), C.byref(nc))
+        if st != OK:
+            raise ElasticError(st, "element colouring failed")
+    finally:
+        L.elx_host_structure_destroy(h)
+    assert col.max() == nc.value
+    return col
 
 
 @dataclass

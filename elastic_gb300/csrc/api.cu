@@ -84,9 +84,8 @@ void upload_structure(elx_ctx *c, bool prederived) {
   }
   std::vector<int32_t> eq(s.id.size());
   for (size_t q = 0; q < eq.size(); q++) eq[q] = s.id[q] - 1;
-  std::vector<int32_t> ia0(s.ia.size()), ja0(s.ja.size());
+  std::vector<int32_t> ia0(s.ia.size());
   for (size_t i = 0; i < ia0.size(); i++) ia0[i] = s.ia[i] - 1;
-  for (size_t i = 0; i < ja0.size(); i++) ja0[i] = s.ja[i] - 1;
   c->upload(c->conn, conn.data(), conn.size());
   c->upload(c->mat, mat.data(), mat.size());
   c->upload(c->elnum, elnum.data(), elnum.size());
@@ -95,10 +94,9 @@ void upload_structure(elx_ctx *c, bool prederived) {
   c->upload(c->eq, eq.data(), eq.size());
   c->upload(c->e, m.e.data(), m.e.size());
   c->upload(c->ia, ia0.data(), ia0.size());
-  c->upload(c->ja, ja0.data(), ja0.size());
   if (const char *env = getenv("ELX_DELTA16")) c->use_delta = atoi(env) != 0;
   if (const char *env = getenv("ELX_GATHER_BLOCKS")) c->gather_blocks = atoi(env);
-  if (const char *env = getenv("ELX_GROUP_LANES")) c->group_lanes = atoi(env);
+  if (const char *env = getenv("ELX_SPMM_UNROLL")) c->spmm_unroll = atoi(env);
   c->spmv_kind = elx::kSpmvGather;
   if (const char *env = getenv("ELX_SPMV"))
     c->spmv_kind = std::string(env) == "tile" ? elx::kSpmvTiled : elx::kSpmvGather;
@@ -109,21 +107,63 @@ void upload_structure(elx_ctx *c, bool prederived) {
   c->use_blocks = want_blocks && s.blocked;
   for (DBuf *v : {&c->iat, &c->jat, &c->pt, &c->ja16, &c->jat16, &c->tile_tgt, &c->tile_out,
                   &c->tgt_col, &c->tgt_start, &c->tpos, &c->halo_ptr, &c->halo_slot,
-                  &c->tile_desc, &c->part, &c->alt, &c->bia, &c->bja, &c->bt, &c->bval,
-                  &c->bval32, &c->sell_ptr, &c->sell_col, &c->sell_val, &c->sell_val64,
-                  &c->sell_d16})
+                  &c->tile_desc, &c->part, &c->alt, &c->ja, &c->bia, &c->bt, &c->sell_ptr,
+                  &c->sell_col, &c->sell_val, &c->sell_val64, &c->sell_d16})
     c->release(*v);
   if (c->use_blocks) {
-    // the node-block product replaces both scalar kernel families
+    // the node-block product replaces both scalar kernel families: the
+    // sliced FP64 copy is the only device copy of the full block rows (the
+    // fill reads the CSRC arrays through bia / bt); ja stays on the host
     s.tile_rows = s.ntiles = 0;
     s.bw16 = false;
     c->upload(c->bia, s.bia.data(), s.bia.size());
-    c->upload(c->bja, s.bja.data(), s.bja.size());
     c->upload(c->bt, s.bt.data(), s.bt.size());
-    c->alloc(c->bval, (size_t)s.nnzb * s.bsize * s.bsize * 8 + 64);
+    c->upload(c->sell_ptr, s.sell_ptr.data(), s.sell_ptr.size());
+    c->upload(c->sell_col, s.sell_col.data(), s.sell_col.size());
+    const size_t slots = (size_t)s.sell_ptr[s.nslices] * elx::kSliceRows;
+    const size_t bytes64 = slots * s.bsize * s.bsize * 8;
+    c->alloc(c->sell_val64, bytes64 + 64);
+    int l2 = 0;
+    ELX_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device));
+    // streaming loads unless the copy fits in 60 % of L2 (ELX_SELL_STREAM=0/1
+    // forces either: 49.7 against 54.5 us for the FP32 copy of the 64^3 HEXA8
+    // cube, 277 MB; 17.2 against 12.6 us on the 48^3 TETRA4 mesh, 64 MB)
+    const double colb = (double)slots * 4;
+    c->sell_stream = (double)bytes64 / 2 + colb > 0.6 * l2;
+    c->sell64_stream = (double)bytes64 + colb > 0.6 * l2;
+    if (const char *env = getenv("ELX_SELL_STREAM"))
+      c->sell_stream = c->sell64_stream = atoi(env) != 0;
+    // 16-bit column offsets when every block column is within 32767 block
+    // rows of its row (RCM keeps the bandwidth small): half the index bytes
+    // of a copy streamed from HBM (48.8 against 50.5 us for the FP32 product
+    // on the 64^3 HEXA8 cube; a copy resident in L2 gains nothing: 12.6 us
+    // either way on the 48^3 TETRA4 mesh)
+    if (c->sell_stream) {
+      const int R = elx::kSliceRows;
+      std::vector<int16_t> d16(s.sell_col.size());
+      bool fits = std::getenv("ELX_SELL_D16") == nullptr || std::atoi(std::getenv("ELX_SELL_D16"));
+      for (int sl = 0; sl < s.nslices && fits; sl++)
+        for (int32_t g = s.sell_ptr[sl]; g < s.sell_ptr[sl + 1] && fits; g++)
+          for (int t = 0; t < R; t++) {
+            const int I = sl * R + t;
+            // rows past the matrix (last slice) read the last row's x
+            const int J = I < s.nb ? s.sell_col[(size_t)g * R + t] : s.nb - 1;
+            const int d = J - I;
+            if (d < -32768 || d > 32767) {
+              fits = false;
+              break;
+            }
+            d16[(size_t)g * R + t] = (int16_t)d;
+          }
+      if (fits) c->upload(c->sell_d16, d16.data(), d16.size());
+    }
     c->alloc(c->part, 16);
-
   } else {
+    {
+      std::vector<int32_t> ja0(s.ja.size());
+      for (size_t i = 0; i < ja0.size(); i++) ja0[i] = s.ja[i] - 1;
+      c->upload(c->ja, ja0.data(), ja0.size());
+    }
     choose_tiles(s);
     elx::build_transpose(s);
     c->upload(c->iat, s.iat.data(), s.iat.size());
@@ -149,7 +189,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
   c->alloc(c->ad, n * 8 + 64);
   c->alloc(c->al, nad * 8 + 64);
   for (DBuf *v : {&c->ad32, &c->al32, &c->alt32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32,
-                  &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate})
+                  &c->r0v, &c->tv, &c->unit, &c->gbasis, &c->garrays, &c->gstate})
     c->release(*v);
   release_block(c);
   c->tuned_width[0] = c->tuned_width[1] = 0;
@@ -158,7 +198,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
     c->release(*v);
   c->have_stress = false;
   release_partitions(c);
-  c->have_fp32 = 0;
+  c->have_fp32 = false;
   c->alloc(c->u, (size_t)m.ndf * m.nnode * 8);
   ELX_CUDA(cudaMemsetAsync(c->u.p, 0, c->u.bytes, c->stream));
   c->alloc(c->b0, n * 8);
@@ -167,7 +207,7 @@ void upload_structure(elx_ctx *c, bool prederived) {
   ELX_CUDA(cudaMemsetAsync(c->b.p, 0, c->b.bytes, c->stream));
   c->alloc(c->scal, sizeof(elx::PcgScalars) * 2);
   ELX_CUDA(cudaMemsetAsync(c->scal.p, 0, c->scal.bytes, c->stream));  // slot 1: done = 0
-  c->alloc(c->partials, sizeof(double) * 4 * 4096);
+  c->alloc(c->partials, sizeof(double) * 4 * std::max(4096, elx::grid_cap(32)));
   c->alloc(c->counters, sizeof(unsigned int) * 16);
   ELX_CUDA(cudaMemsetAsync(c->counters.p, 0, c->counters.bytes, c->stream));
   c->alloc(c->flags, sizeof(int32_t) * 4);
@@ -179,15 +219,12 @@ void upload_structure(elx_ctx *c, bool prederived) {
   c->have_matrix = false;
 }
 
-// FP32 copies of the matrix (after each assembly) and the FP32 inner-solver
-// vectors (once per structure), allocated on first use.  With node blocks the
-// single-vector product reads the sliced copy and the block solver the
-// block-major one (`block`); each is made only when its solver asks.
-void ensure_fp32(elx_ctx *c, bool block = false) {
+// FP32 copy of the matrix (after each assembly) and the FP32 inner-solver
+// vectors (once per structure), allocated on first use.  With node blocks
+// the single-vector and the block products both read the sliced FP32 copy,
+// filled straight from ad / al.
+void ensure_fp32(elx_ctx *c) {
   const size_t n = (size_t)c->s.neq, nad = (size_t)c->s.nad;
-  // the lane-group product (group_lanes > 0) reads the block-major copy too
-  block = block || c->group_lanes > 0;
-  const int want = block ? kFp32Block : kFp32Single;
   if (!c->m32.p) {
     if (!c->use_blocks) {
       c->alloc(c->ad32, n * 4 + 64);
@@ -197,96 +234,29 @@ void ensure_fp32(elx_ctx *c, bool block = false) {
     for (DBuf *v : {&c->m32, &c->p32, &c->q32, &c->r32, &c->x32}) c->alloc(*v, n * 4 + 64);
     c->drop_graphs();
   }
-  if (c->use_blocks && block && !c->bval32.p) {
-    c->alloc(c->bval32, (size_t)c->s.nnzb * c->s.bsize * c->s.bsize * 4 + 64);
+  if (c->use_blocks && !c->sell_val.p) {
+    c->alloc(c->sell_val, (size_t)c->s.sell_ptr[c->s.nslices] * elx::kSliceRows *
+                                  c->s.bsize * c->s.bsize * 4 + 64);
     c->drop_graphs();
   }
-  if (c->use_blocks && !block && !c->sell_val.p) {
-    if (!c->sell_col.p) {
-      c->upload(c->sell_ptr, c->s.sell_ptr.data(), c->s.sell_ptr.size());
-      c->upload(c->sell_col, c->s.sell_col.data(), c->s.sell_col.size());
-    }
-    const size_t bytes =
-        (size_t)c->s.sell_ptr[c->s.nslices] * elx::kSliceRows * c->s.bsize * c->s.bsize * 4;
-    c->alloc(c->sell_val, bytes + 64);
-    int l2 = 0;
-    ELX_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device));
-    c->sell_stream = (double)(bytes + c->sell_col.bytes) > 0.6 * l2;
-    if (const char *env = getenv("ELX_SELL_STREAM")) c->sell_stream = atoi(env) != 0;
-    // 16-bit column offsets when every block column is within 32767 block
-    // rows of its row (RCM keeps the bandwidth small): half the index bytes
-    // of a copy streamed from HBM (48.8 against 50.5 us on the 64^3 HEXA8
-    // cube; a copy resident in L2 gains nothing: 12.6 us either way on the
-    // 48^3 TETRA4 mesh)
-    if (c->sell_stream) {
-      const elx::Structure &s = c->s;
-      const int R = elx::kSliceRows;
-      std::vector<int16_t> d16(s.sell_col.size());
-      bool fits = std::getenv("ELX_SELL_D16") == nullptr || std::atoi(std::getenv("ELX_SELL_D16"));
-      for (int sl = 0; sl < s.nslices && fits; sl++)
-        for (int32_t g = s.sell_ptr[sl]; g < s.sell_ptr[sl + 1] && fits; g++)
-          for (int t = 0; t < R; t++) {
-            const int I = sl * R + t;
-            // rows past the matrix (last slice) read the last row's x
-            const int J = I < s.nb ? s.sell_col[(size_t)g * R + t] : s.nb - 1;
-            const int d = J - I;
-            if (d < -32768 || d > 32767) {
-              fits = false;
-              break;
-            }
-            d16[(size_t)g * R + t] = (int16_t)d;
-          }
-      if (fits) c->upload(c->sell_d16, d16.data(), d16.size());
-    }
-    c->drop_graphs();
-  }
-  if (c->have_fp32 & want) return;
+  if (c->have_fp32) return;
   if (!c->use_blocks) {
     elx::launch_demote_values(c->csrc_dev(), c->stream);
     c->launches += c->s.nad ? 2 : 1;
-    c->have_fp32 |= kFp32Single | kFp32Block;
   } else {
-    if (block)
-      elx::launch_demote_blocks(c->csrc_dev(), c->stream);
-    else
-      elx::launch_demote_sell(c->csrc_dev(), c->stream);
-    c->launches += 1;
-    c->have_fp32 |= want;
-  }
-}
-
-// The kernel-side copies of a new CSRC matrix: the node blocks, or the
-// transposed upper values of the gather.
-// The sliced FP64 copy of the node blocks for the single-vector FP64
-// product (made on first use, then refreshed after every assembly): 126
-// against 133 us per product on the 64^3 HEXA8 cube and 39.4 against 47.4 us
-// on the 48^3 TETRA4 mesh, for the FP64 matrix bytes once more
-// (ELX_SELL64=0 keeps the block-major product).
-void ensure_sell64(elx_ctx *c) {
-  if (!c->use_blocks || c->sell_val64.p) return;
-  if (const char *env = getenv("ELX_SELL64"); env && atoi(env) == 0) return;
-  if (!c->sell_col.p) {
-    c->upload(c->sell_ptr, c->s.sell_ptr.data(), c->s.sell_ptr.size());
-    c->upload(c->sell_col, c->s.sell_col.data(), c->s.sell_col.size());
-  }
-  c->alloc(c->sell_val64, (size_t)c->s.sell_ptr[c->s.nslices] * elx::kSliceRows * c->s.bsize *
-                                  c->s.bsize * 8 + 64);
-  c->drop_graphs();
-  if (c->have_matrix) {
-    elx::launch_copy_sell64(c->csrc_dev(), c->stream);
+    elx::launch_fill_sell32(c->csrc_dev(), c->stream);
     c->launches += 1;
   }
+  c->have_fp32 = true;
 }
 
+// The kernel-side copies of a new CSRC matrix: the sliced FP64 node blocks,
+// or the transposed upper values of the gather.
 void refresh_derived_values(elx_ctx *c) {
   const elx::CsrcDev k = c->csrc_dev();
   if (c->use_blocks) {
-    elx::launch_fill_blocks(k, c->stream);
-    c->launches += 2;
-    if (c->sell_val64.p) {
-      elx::launch_copy_sell64(k, c->stream);
-      c->launches += 1;
-    }
+    elx::launch_fill_sell64(k, c->stream);
+    c->launches += 1;
   } else if (c->s.nad) {
     elx::launch_transpose_values(k, c->stream);
     c->launches += 1;
@@ -311,7 +281,7 @@ void assemble_resident(elx_ctx *c) {
   c->launches += (int64_t)s.segments.size();
   ELX_CUDA(cudaMemcpyAsync(c->h_flags, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
   c->sync();
-  c->have_fp32 = 0;
+  c->have_fp32 = false;
   if (c->h_flags[0] != INT_MAX) {
     c->have_matrix = false;
     throw Error{ELX_ERR_BAD_DET, "non-positive Jacobian determinant in element " +
@@ -567,7 +537,10 @@ void pcg_mixed(elx_ctx *c, double tol, int maxit, elx_info *info) {
 }
 
 // pbicgstab (Iters.f:1079-1349) on the device: right Jacobi, 2-norm test.
-void bicgstab64(elx_ctx *c, double tol, int maxit, elx_info *info) {
+// With plain, bicgstab (Iters.f:812-1075): the same iteration with M = I (a
+// vector of ones: z = 1 * p is p exactly), whose beta from (r, b) equals the
+// (r, r0) of pbicgstab because x0 = 0 makes r0 = b exactly.
+void bicgstab64(elx_ctx *c, double tol, int maxit, elx_info *info, bool plain) {
   auto t0 = std::chrono::steady_clock::now();
   const size_t n = (size_t)c->s.neq;
   if (!c->r0v.p) {
@@ -575,10 +548,21 @@ void bicgstab64(elx_ctx *c, double tol, int maxit, elx_info *info) {
     c->alloc(c->tv, n * 8);
     c->drop_graphs();
   }
-  build_preconditioner(c);
+  if (plain && !c->unit.p) {
+    const std::vector<double> one(n, 1.0);
+    c->upload(c->unit, one.data(), n);
+    c->sync();
+  }
+  build_preconditioner(c);  // the zero-diagonal check of Iters.f:900-905 too
+  const double *m = plain ? c->unit.as<double>() : c->m.as<double>();
+  if (c->bicg_graph && c->bicg_plain != plain) {
+    cudaGraphExecDestroy(c->bicg_graph);
+    c->bicg_graph = nullptr;
+  }
+  c->bicg_plain = plain;
   set_scalars(c, tol, maxit);
   auto *sc = c->scal.as<elx::PcgScalars>();
-  elx::launch_bicg_start(c->s.neq, c->b.as<double>(), c->m.as<double>(), c->xs.as<double>(),
+  elx::launch_bicg_start(c->s.neq, c->b.as<double>(), m, c->xs.as<double>(),
                          c->r.as<double>(), c->r0v.as<double>(), c->p.as<double>(),
                          c->z.as<double>(), sc, c->partials.as<double>(),
                          c->counters.as<unsigned int>() + 2, c->stream);
@@ -588,7 +572,7 @@ void bicgstab64(elx_ctx *c, double tol, int maxit, elx_info *info) {
     ELX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     try {
       for (int i = 0; i < kBatch; i++)
-        elx::launch_bicg_iteration(c->csrc_dev(), c->m.as<double>(), c->xs.as<double>(),
+        elx::launch_bicg_iteration(c->csrc_dev(), m, c->xs.as<double>(),
                                    c->r.as<double>(), c->r0v.as<double>(), c->p.as<double>(),
                                    c->z.as<double>(), c->q.as<double>(), c->tv.as<double>(), sc,
                                    c->partials.as<double>(), c->counters.as<unsigned int>() + 6,
@@ -608,7 +592,10 @@ void bicgstab64(elx_ctx *c, double tol, int maxit, elx_info *info) {
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (!last.done) last.status = ELX_ERR_NO_CONVERGENCE;
   fill_info(c, info, last, secs);
-  if (info) info->mflops = 0.0;
+  if (info) {
+    info->mflops = 0.0;
+    if (plain) info->norm_m_r = info->norm_r;  // no M: the 2-norm residual
+  }
   if (last.status != ELX_OK)
     throw Error{last.status, "BiCGSTAB: no convergence after " + std::to_string(last.iters) +
                                  " iterations"};
@@ -699,7 +686,7 @@ void ensure_block(elx_ctx *c, int cap, bool mixed) {
       c->alloc(*v, n * cap * 8);
     c->alloc(c->bk_cols, sizeof(elx::ColScalars) * kMaxBlockWidth);
     c->alloc(c->bk_hdr, sizeof(elx::BlockHeader) * 2);
-    c->alloc(c->bk_part, sizeof(double) * 2 * kMaxBlockWidth * 1216);
+    c->alloc(c->bk_part, sizeof(double) * 2 * kMaxBlockWidth * elx::grid_cap(8));
     c->alloc(c->bk_cnt, sizeof(unsigned int) * 8);
     ELX_CUDA(cudaMemsetAsync(c->bk_cnt.p, 0, c->bk_cnt.bytes, c->stream));
     c->alloc(c->bk_diag, sizeof(double) * 4 * kMaxBlockWidth);
@@ -743,7 +730,7 @@ int autotune_block_width(elx_ctx *c, bool mixed, double *times_us = nullptr) {
   const int slot = mixed ? 1 : 0;
   if (c->tuned_width[slot] && !times_us) return c->tuned_width[slot];
   ensure_block(c, kMaxBlockWidth, mixed);
-  if (mixed) ensure_fp32(c, true);
+  if (mixed) ensure_fp32(c);
   const size_t n = (size_t)c->s.neq;
   ELX_CUDA(cudaMemsetAsync(c->bk_p.p, 0, n * kMaxBlockWidth * 8, c->stream));
   if (mixed) ELX_CUDA(cudaMemsetAsync(c->bk_p32.p, 0, n * kMaxBlockWidth * 4, c->stream));
@@ -793,7 +780,7 @@ void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int
           "block solves need node blocks (every node all free or all fixed)");
   const bool mixed = precision == ELX_PREC_MIXED;
   auto t0 = std::chrono::steady_clock::now();
-  if (mixed) ensure_fp32(c, true);
+  if (mixed) ensure_fp32(c);
   build_preconditioner(c);
   if (width == 0) width = autotune_block_width(c, mixed);
   int w = 1;
@@ -936,7 +923,6 @@ void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit
   require(c->have_matrix, ELX_ERR_STATE, "solve before the matrix is assembled");
   require(tol > 0 && maxit >= 0, ELX_ERR_ARG, "tol must be > 0 and maxit >= 0");
   if (info) std::memset(info, 0, sizeof(*info));
-  ensure_sell64(c);
   if (solver == ELX_SOLVER_PCG && precision == ELX_PREC_FP64) {
     pcg64(c, tol, maxit, info);
     return;
@@ -945,8 +931,9 @@ void solve_resident(elx_ctx *c, int solver, int precision, double tol, int maxit
     pcg_mixed(c, tol, maxit, info);
     return;
   }
-  if (solver == ELX_SOLVER_BICGSTAB && precision == ELX_PREC_FP64) {
-    bicgstab64(c, tol, maxit, info);
+  if ((solver == ELX_SOLVER_BICGSTAB || solver == ELX_SOLVER_BICGSTAB_NOPREC) &&
+      precision == ELX_PREC_FP64) {
+    bicgstab64(c, tol, maxit, info, solver == ELX_SOLVER_BICGSTAB_NOPREC);
     return;
   }
   if (solver == ELX_SOLVER_GMRES && precision == ELX_PREC_FP64) {
@@ -1020,6 +1007,16 @@ extern "C" {
 
 const char *elx_version(void) { return "elastic_gb300 0.1 (sm_103a)"; }
 
+int elx_fp64_fma_rate(int32_t device, double *fma_per_s, double *per_clock_per_sm) {
+  if (!fma_per_s) return ELX_ERR_ARG;
+  try {
+    *fma_per_s = elx::measure_fp64_fma_rate(device, per_clock_per_sm);
+    return ELX_OK;
+  } catch (const Error &e) {
+    return e.code;
+  }
+}
+
 int elx_create(elx_ctx **out, const elx_opts *opts) {
   if (!out) return ELX_ERR_ARG;
   *out = nullptr;
@@ -1061,8 +1058,8 @@ void elx_destroy(elx_ctx *c) {
                   &c->tile_tgt, &c->tile_out, &c->tgt_col, &c->tgt_start, &c->tpos,
                   &c->halo_ptr, &c->halo_slot, &c->tile_desc, &c->part, &c->ad, &c->al,
                   &c->ad32, &c->al32, &c->m32, &c->p32, &c->q32, &c->r32, &c->x32,
-                  &c->r0v, &c->tv, &c->gbasis, &c->garrays, &c->gstate,
-                  &c->bia, &c->bja, &c->bt, &c->bval, &c->bval32, &c->sell_ptr, &c->sell_col,
+                  &c->r0v, &c->tv, &c->unit, &c->gbasis, &c->garrays, &c->gstate,
+                  &c->bia, &c->bt, &c->sell_ptr, &c->sell_col,
                   &c->sell_val, &c->sell_val64, &c->sell_d16,
                   &c->node_count, &c->tstress, &c->tx0buf, &c->fbuf, &c->ld_node, &c->ld_ptr,
                   &c->ld_ent, &c->ld_vec, &c->vtkbuf,
@@ -1143,6 +1140,7 @@ int elx_build_structure(elx_ctx *c, const int32_t *bc, int32_t reorder) {
 
 struct elx_host_structure {
   elx::Structure s;
+  elx::Mesh m;  // connectivity only (coordinates and materials zero)
   int ndf = 0;
   std::string err;
 };
@@ -1160,6 +1158,7 @@ int elx_host_structure_create(elx_host_structure **out, int32_t ndm, int32_t ndf
     auto *h = new elx_host_structure();
     h->ndf = ndf;
     build_host_structure(m, bc, reorder != 0, h->s);
+    h->m = std::move(m);
     *out = h;
     return ELX_OK;
   } catch (const Error &e) {
@@ -1233,6 +1232,20 @@ int elx_host_structure_get(const elx_host_structure *h, int32_t *perm, int32_t *
   if (ia) std::copy(s.ia.begin(), s.ia.end(), ia);
   if (ja) std::copy(s.ja.begin(), s.ja.end(), ja);
   return ELX_OK;
+}
+
+int elx_host_structure_colors(const elx_host_structure *h, int32_t *elcolor, int32_t *ncolors) {
+  if (!h) return ELX_ERR_ARG;
+  try {
+    std::vector<int32_t> color;
+    const int n = elx::color_elements(h->m, color);
+    if (ncolors) *ncolors = n;
+    if (elcolor)
+      for (size_t el = 0; el < color.size(); el++) elcolor[el] = color[el] + 1;
+    return ELX_OK;
+  } catch (const std::bad_alloc &) {
+    return ELX_ERR_OOM;
+  }
 }
 
 void elx_host_structure_destroy(elx_host_structure *h) { delete h; }
@@ -1370,7 +1383,7 @@ int elx_set_matrix(elx_ctx *c, const double *ad, const double *al) {
     refresh_derived_values(c);
     c->sync();
     c->have_matrix = true;
-    c->have_fp32 = 0;
+    c->have_fp32 = false;
   });
 }
 
@@ -1631,7 +1644,6 @@ int elx_spmv(elx_ctx *c, int32_t precision, const double *x, double *y) {
     const size_t n = (size_t)c->s.neq;
     ELX_CUDA(cudaMemcpyAsync(c->p.p, x, n * 8, cudaMemcpyHostToDevice, c->stream));
     if (precision == ELX_PREC_FP64) {
-      ensure_sell64(c);
       spmv64(c, c->p.as<double>(), c->q.as<double>());
     } else if (precision == ELX_PREC_MIXED) {
       // the FP32 product of the mixed-precision inner iteration
@@ -1658,7 +1670,6 @@ int elx_spmv_resident(elx_ctx *c, int32_t precision, int32_t reps) {
     set_scalars(c, 0.0, 0);
     auto *sc = c->scal.as<elx::PcgScalars>();
     if (precision == ELX_PREC_FP64) {
-      ensure_sell64(c);
       for (int i = 0; i < reps; i++) {
         if (c->spmv_kind == elx::kSpmvTiled) {
           spmv64(c, c->p.as<double>(), c->q.as<double>());

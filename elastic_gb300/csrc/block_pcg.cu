@@ -28,6 +28,7 @@
 #include "elx_krylov.h"
 #include "elx_ptx.cuh"
 #include "elx_reduce.cuh"
+#include "elx_sell.cuh"
 
 namespace elx {
 namespace {
@@ -137,23 +138,6 @@ template <class T, int VC>
 struct ColVec {
   T v[VC];
 };
-// 16-byte column loads issued in program order (volatile; see spmm_kernel)
-template <class T, int VC>
-__device__ __forceinline__ ColVec<T, VC> load_cols_ordered(const T *p) {
-  ColVec<T, VC> r;
-  if constexpr (VC * sizeof(T) == 16 && sizeof(T) == 4) {
-    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
-                 : "=f"(r.v[0]), "=f"(r.v[1]), "=f"(r.v[2]), "=f"(r.v[3])
-                 : "l"(p));
-  } else if constexpr (VC * sizeof(T) == 16) {
-    asm volatile("ld.global.nc.v2.f64 {%0, %1}, [%2];" : "=d"(r.v[0]), "=d"(r.v[1]) : "l"(p));
-  } else {
-#pragma unroll
-    for (int j = 0; j < VC; j++) r.v[j] = ptx::ld_nc_ordered(p + j);
-  }
-  return r;
-}
-
 template <class T, int VC>
 __device__ __forceinline__ ColVec<T, VC> load_cols(const T *p) {
   ColVec<T, VC> r;
@@ -223,94 +207,100 @@ __device__ __forceinline__ bool column_reduce_v(double (&v)[VC], double *partial
   return true;
 }
 
-// Y = K X for W columns: a group of G = W / VC lanes per block row, each lane
-// on VC consecutive columns (one 16-byte load per x row at most).  The lanes
-// of a group load each block's column index and B^2 values once (the same
-// address in all G lanes); every value then feeds VC FMAs per lane.  With
-// DOT, also pq_c = (x_c, y_c) and alpha_c = d_c / pq_c for the active
-// columns.  A launch with gate != nullptr runs only while *gate != 0.
-template <class T, int B, int W, bool DOT, bool MASK = false, int U = 1>
-__global__ void __launch_bounds__(kThreads)
-spmm_kernel(int nb, const int32_t *__restrict__ bia, const int32_t *__restrict__ bja,
-            const T *__restrict__ bval, const T *__restrict__ X, T *__restrict__ Y,
-            ColScalars *cols, BlockHeader *hdr, double *partials, unsigned int *counter,
-            const int32_t *gate) {
+// Y = K X for W columns on a sliced copy of the node blocks.  A group of
+// G = W / VC lanes works on one block row, each lane on VC consecutive
+// columns (one 16-byte x load per row of a block); G warps take one slice
+// (kSliceRows block rows).  The G lanes of a row load its block with the same
+// 16-byte chunk loads (a broadcast), so one warp's load of a chunk covers
+// 32 / G consecutive slots: 512 / G contiguous bytes, where the block-major
+// form read each block as B^2 scalar loads at a 36-byte stride.  Every lane
+// of a slice walks the slice's width; U slot groups' matrix loads are issued
+// together, then each group's x loads and FMAs, whose order per row is the
+// block order (the sums do not depend on U).  Padding slots hold zero
+// blocks and the row's own column.  With DOT, also pq_c = (x_c, y_c) and
+// alpha_c = d_c / pq_c for the active columns; a launch with gate != nullptr
+// runs only while *gate != 0; with MASK only the lanes whose columns asked
+// for a residual replacement compute.
+template <class T, int B, int W, bool DOT, bool MASK, int U, bool LD, bool D16>
+__global__ void __launch_bounds__(kThreads, 3)
+sell_spmm_kernel(int nb, int nslices, const int32_t *__restrict__ sell_ptr,
+                 const int32_t *__restrict__ sell_col, const int16_t *__restrict__ col16,
+                 const T *__restrict__ sval, const T *__restrict__ X, T *__restrict__ Y,
+                 ColScalars *cols, BlockHeader *hdr, double *partials, unsigned int *counter,
+                 const int32_t *gate) {
   constexpr int VC = (16 / (int)sizeof(T)) < W ? (16 / (int)sizeof(T)) : W;
   constexpr int G = W / VC;
-  constexpr int BB = B * B;
+  constexpr int BB = B * B, R = kSliceRows;
+  constexpr int SPC = kThreads / (R * G);  // slices per CTA pass
+  static_assert(SPC >= 1, "a CTA must hold a whole slice");
   if (hdr->active == 0) return;
   if (gate && *gate == 0) return;
   const int c0 = (threadIdx.x % G) * VC;
+  const int t = (threadIdx.x / G) % R;
   if constexpr (MASK) {
-    // only the columns that asked for a residual replacement
     bool need = false;
 #pragma unroll
     for (int j = 0; j < VC; j++) need = need || (!cols[c0 + j].done && cols[c0 + j].update);
     if (!need) return;
   }
-  const int ngroups = gridDim.x * (kThreads / G);
   T v[VC];  // this thread's share of (x_c, y_c), in T (the FP64 pipe is narrow)
 #pragma unroll
   for (int j = 0; j < VC; j++) v[j] = T(0);
-  for (int I = (blockIdx.x * kThreads + threadIdx.x) / G; I < nb; I += ngroups) {
-    const int pb = bia[I], pe = bia[I + 1];
+  // passes of SPC slices, every gridDim.x-th for this CTA (contiguous runs
+  // of passes per CTA measured slower: 265 against 247 us, W = 16 FP32 on the
+  // 96x96x48 plate)
+  for (int sl = blockIdx.x * SPC + (int)threadIdx.x / (R * G); sl < nslices;
+       sl += gridDim.x * SPC) {
+    const int g0 = sell_ptr[sl], g1 = sell_ptr[sl + 1];
     T acc[B][VC];
 #pragma unroll
     for (int a = 0; a < B; a++)
 #pragma unroll
       for (int j = 0; j < VC; j++) acc[a][j] = T(0);
-    // U blocks per step, all their loads issued before their FMAs (the
-    // FMAs keep the one-block order: the same sums bitwise)
-    int p = pb;
-    for (; p + U <= pe; p += U) {
+    for (int g = g0; g < g1; g += U) {
+      const int nu = min(U, g1 - g);
       int J[U];
       T bv[U][BB];
-      ColVec<T, VC> xv[U][B];
-#pragma unroll
-      for (int u = 0; u < U; u++) J[u] = U > 1 ? ptx::ld_nc_ordered(bja + p + u) : bja[p + u];
 #pragma unroll
       for (int u = 0; u < U; u++)
-#pragma unroll
-        for (int e = 0; e < BB; e++)
-          bv[u][e] = U > 1 ? ptx::ld_nc_ordered(bval + (size_t)(p + u) * BB + e)
-                           : bval[(size_t)(p + u) * BB + e];
+        if (u < nu) J[u] = sell_column<D16, LD>(sell_col, col16, sl, g + u, t);
 #pragma unroll
       for (int u = 0; u < U; u++)
-#pragma unroll
-        for (int b = 0; b < B; b++)
-          xv[u][b] = U > 1 ? load_cols_ordered<T, VC>(X + (size_t)(J[u] * B + b) * W + c0)
-                           : load_cols<T, VC>(X + (size_t)(J[u] * B + b) * W + c0);
+        if (u < nu) sell_load<T, B, LD>(sval + (size_t)(g + u) * BB * R, t, bv[u]);
+      // x of each group loaded just before its FMAs (mostly L1 hits): the
+      // registers go to more groups of matrix loads in flight (244 against
+      // 299.5 us for W = 16 FP32 on the 96x96x48 plate with all loads issued
+      // first; 3 groups at 3 CTAs per SM measured best of 3 / 4 / 6 / 8
+      // groups at 1-3 CTAs per SM, 244-301 us)
 #pragma unroll
       for (int u = 0; u < U; u++)
-#pragma unroll
-        for (int a = 0; a < B; a++)
+        if (u < nu) {
+          ColVec<T, VC> xw[B];
 #pragma unroll
           for (int b = 0; b < B; b++)
+            xw[b] = load_cols<T, VC>(X + (size_t)(J[u] * B + b) * W + c0);
 #pragma unroll
-            for (int j = 0; j < VC; j++) acc[a][j] += bv[u][a * B + b] * xv[u][b].v[j];
+          for (int a = 0; a < B; a++)
+#pragma unroll
+            for (int b = 0; b < B; b++)
+#pragma unroll
+              for (int j = 0; j < VC; j++) acc[a][j] += bv[u][a * B + b] * xw[b].v[j];
+        }
     }
-    for (; p < pe; p++) {
-      const int J = bja[p];
-      T bv[BB];
+    const int I = sl * R + t;
+    if (I < nb) {
 #pragma unroll
-      for (int e = 0; e < BB; e++) bv[e] = bval[(size_t)p * BB + e];
-      ColVec<T, VC> xv[B];
+      for (int a = 0; a < B; a++) {
+        const size_t q = (size_t)(I * B + a) * W + c0;
+        ColVec<T, VC> yv;
 #pragma unroll
-      for (int b = 0; b < B; b++) xv[b] = load_cols<T, VC>(X + (size_t)(J * B + b) * W + c0);
+        for (int j = 0; j < VC; j++) yv.v[j] = acc[a][j];
+        store_cols<T, VC>(Y + q, yv);
+        if (DOT) {
+          const ColVec<T, VC> xq = load_cols<T, VC>(X + q);
 #pragma unroll
-      for (int a = 0; a < B; a++)
-#pragma unroll
-        for (int b = 0; b < B; b++)
-#pragma unroll
-          for (int j = 0; j < VC; j++) acc[a][j] += bv[a * B + b] * xv[b].v[j];
-    }
-#pragma unroll
-    for (int a = 0; a < B; a++) {
-      const size_t q = (size_t)(I * B + a) * W + c0;
-#pragma unroll
-      for (int j = 0; j < VC; j++) {
-        Y[q + j] = acc[a][j];
-        if (DOT) v[j] += X[q + j] * acc[a][j];
+          for (int j = 0; j < VC; j++) v[j] += xq.v[j] * acc[a][j];
+        }
       }
     }
   }
@@ -704,45 +694,72 @@ __global__ void deinterleave_kernel(int n, int w, const double *__restrict__ int
 int bgrid(size_t nw) {
   const size_t g = (nw + kThreads - 1) / kThreads;
   // multi-vectors of W columns keep eight blocks per SM busy (29.9 / 31.6 /
-  // 37.6 ms per load case at 1216 / 608 / 304 blocks, 96x96x48 plate)
-  return (int)std::max<size_t>(1, std::min<size_t>(g, 1216));
+  // 37.6 ms per load case at 8 / 4 / 2 blocks per SM, 96x96x48 plate)
+  return (int)std::max<size_t>(1, std::min<size_t>(g, (size_t)grid_cap(8)));
 }
 
+// Y = K X on the sliced copy of precision T: one CTA pass per SPC slices,
+// at most the context's grid bound (the partial sums of the dots hold one
+// row per CTA).
 template <class T, int W>
-void spmm_w(const CsrcDev &k, const T *val, const T *X, T *Y, ColScalars *cols, BlockHeader *hdr,
+void spmm_w(const CsrcDev &k, const T *X, T *Y, ColScalars *cols, BlockHeader *hdr,
             double *partials, unsigned int *counter, const int32_t *gate, bool dot,
-            cudaStream_t st, bool mask = false) {
+            cudaStream_t st) {
   constexpr int VC = (16 / (int)sizeof(T)) < W ? (16 / (int)sizeof(T)) : W;
-  const int grid = std::max(1, std::min((k.nb * (W / VC) + kThreads - 1) / kThreads, 1216));
-  if (mask) {
-    if (k.bsize == 3)
-      spmm_kernel<T, 3, W, false, true><<<grid, kThreads, 0, st>>>(
-          k.nb, k.bia, k.bja, val, X, Y, cols, hdr, partials, counter, gate);
-    else
-      spmm_kernel<T, 2, W, false, true><<<grid, kThreads, 0, st>>>(
-          k.nb, k.bia, k.bja, val, X, Y, cols, hdr, partials, counter, gate);
-    return;
+  constexpr int SPC = kThreads / (kSliceRows * (W / VC));
+  const T *val;
+  bool ld;
+  if constexpr (sizeof(T) == 4) {
+    val = k.sell_val;
+    ld = k.sell_stream;
+  } else {
+    val = k.sell_val64;
+    ld = k.sell64_stream;
   }
+  ELX_REQUIRE(val != nullptr && k.sell_ptr != nullptr, ELX_ERR_STATE,
+              "sliced node blocks missing for the block product");
+  const bool d16 = k.sell_d16 != nullptr;
+  const int grid = std::max(1, std::min((k.nslices + SPC - 1) / SPC, k.max_grid));
+  // FP32: three slot groups' matrix loads per step; FP64 (FP64-pipe
+  // bound): one
+  const int u = k.spmm_unroll > 0 ? k.spmm_unroll : (sizeof(T) == 4 ? 3 : 1);
+#define ELX_SPMM(B_, DOT_, U_, LD_, D16_)                                                  \
+  do {                                                                                      \
+    sell_spmm_kernel<T, B_, W, DOT_, false, U_, LD_, D16_><<<grid, kThreads, 0, st>>>(      \
+        k.nb, k.nslices, k.sell_ptr, k.sell_col, k.sell_d16, val, X, Y, cols, hdr, partials, \
+        counter, gate);                                                                     \
+  } while (0)
+#define ELX_SPMM_LD(B_, DOT_, U_)           \
+  if (ld && d16)                            \
+    ELX_SPMM(B_, DOT_, U_, true, true);     \
+  else if (ld)                              \
+    ELX_SPMM(B_, DOT_, U_, true, false);    \
+  else if (d16)                             \
+    ELX_SPMM(B_, DOT_, U_, false, true);    \
+  else                                      \
+    ELX_SPMM(B_, DOT_, U_, false, false)
   if (k.bsize == 3) {
-    // 3 blocks in flight per step: 320 against 342 (2) and 339 (1) us for
-    // the W = 16 FP32 product with its dots on the 96x96x48 plate; 29.8
-    // against 31.1 and 33.6 ms per load case for the whole block solve
-#define ELX_SPMM(DOT_, U_)                                                                  \
-  spmm_kernel<T, 3, W, DOT_, false, U_><<<grid, kThreads, 0, st>>>(                          \
-      k.nb, k.bia, k.bja, val, X, Y, cols, hdr, partials, counter, gate)
-    if (dot)
-      ELX_SPMM(true, 3);
-    else
-      ELX_SPMM(false, 3);
-#undef ELX_SPMM
+    if (dot) {
+      if (u >= 3)
+        ELX_SPMM_LD(3, true, 3);
+      else if (u == 2)
+        ELX_SPMM_LD(3, true, 2);
+      else
+        ELX_SPMM_LD(3, true, 1);
+    } else {
+      if (u >= 3)
+        ELX_SPMM_LD(3, false, 3);
+      else
+        ELX_SPMM_LD(3, false, 1);
+    }
   } else {
     if (dot)
-      spmm_kernel<T, 2, W, true><<<grid, kThreads, 0, st>>>(k.nb, k.bia, k.bja, val, X, Y, cols,
-                                                            hdr, partials, counter, gate);
+      ELX_SPMM_LD(2, true, 2);
     else
-      spmm_kernel<T, 2, W, false><<<grid, kThreads, 0, st>>>(k.nb, k.bia, k.bja, val, X, Y, cols,
-                                                             hdr, partials, counter, gate);
+      ELX_SPMM_LD(2, false, 2);
   }
+#undef ELX_SPMM_LD
+#undef ELX_SPMM
 }
 
 template <int W>
@@ -752,12 +769,12 @@ void iteration_w(const CsrcDev &k, const BlockVecs &v, bool mixed, bool replacem
   const int g = bgrid((size_t)n * W);
   unsigned int *cnt = v.counters;
   if (!mixed) {
-    spmm_w<double, W>(k, k.bval, v.p, v.q, v.cols, v.hdr, v.partials, cnt + 0, nullptr, true, st);
+    spmm_w<double, W>(k, v.p, v.q, v.cols, v.hdr, v.partials, cnt + 0, nullptr, true, st);
     bpcg_update_kernel<W><<<g, kThreads, 0, st>>>(n, v.p, v.q, v.m, v.x, v.r, v.cols, v.hdr,
                                                   v.partials, cnt + 1);
     bpcg_direction_kernel<double, W><<<g, kThreads, 0, st>>>(n, v.r, v.m, v.p, v.cols, v.hdr);
   } else {
-    spmm_w<float, W>(k, k.bval32, v.p32, v.q32, v.cols, v.hdr, v.partials, cnt + 0, nullptr, true,
+    spmm_w<float, W>(k, v.p32, v.q32, v.cols, v.hdr, v.partials, cnt + 0, nullptr, true,
                      st);
     brel_update_kernel<W><<<g, kThreads, 0, st>>>(n, v.p32, v.q32, v.m32, v.xlo, v.r32, v.cols,
                                                   v.hdr, v.partials, cnt + 1);
@@ -765,7 +782,7 @@ void iteration_w(const CsrcDev &k, const BlockVecs &v, bool mixed, bool replacem
                                                             v.hdr);
     if (replacement_point) {
       brel_accumulate_kernel<W><<<g, kThreads, 0, st>>>(n, v.x, v.xlo, v.cols, v.hdr);
-      spmm_w<double, W>(k, k.bval, v.x, v.z, v.cols, v.hdr, v.partials, cnt + 2,
+      spmm_w<double, W>(k, v.x, v.z, v.cols, v.hdr, v.partials, cnt + 2,
                         &v.hdr->any_update, false, st);
       brel_residual_kernel<W><<<g, kThreads, 0, st>>>(n, v.b, v.z, v.m, v.r32, v.cols, v.hdr,
                                                       v.partials, cnt + 3);
@@ -792,7 +809,7 @@ void diag_w(const CsrcDev &k, const BlockVecs &v, double *out, cudaStream_t st) 
   const int n = k.neq;
   const int g = bgrid((size_t)n * W);
   // z = K x with the gate open (active may be 0 after the solve)
-  spmm_w<double, W>(k, k.bval, v.x, v.z, v.cols, v.hdr_on, v.partials, v.counters + 5, nullptr,
+  spmm_w<double, W>(k, v.x, v.z, v.cols, v.hdr_on, v.partials, v.counters + 5, nullptr,
                     false, st);
   bdiag_kernel<W><<<g, kThreads, 0, st>>>(n, v.x, v.z, out, v.partials, v.counters + 5);
   bdiag_res_kernel<W><<<g, kThreads, 0, st>>>(n, v.z, v.b, v.m, out, v.partials,
@@ -838,7 +855,7 @@ void launch_block_diagnostics(const CsrcDev &k, const BlockVecs &v, double *out,
 // dots), on the block vectors before the solve initialises its scalars.
 void launch_spmm32(const CsrcDev &k, const BlockVecs &v, cudaStream_t st) {
 #define CALL(W)                                                                                \
-  spmm_w<float, W>(k, k.bval32, v.p32, v.q32, v.cols, v.hdr_on, v.partials, v.counters + 6, \
+  spmm_w<float, W>(k, v.p32, v.q32, v.cols, v.hdr_on, v.partials, v.counters + 6, \
                    nullptr, true, st)
   ELX_W_DISPATCH(v.w, CALL)
 #undef CALL
@@ -847,7 +864,7 @@ void launch_spmm32(const CsrcDev &k, const BlockVecs &v, cudaStream_t st) {
 
 void launch_spmm64(const CsrcDev &k, const BlockVecs &v, cudaStream_t st) {
 #define CALL(W)                                                                            \
-  spmm_w<double, W>(k, k.bval, v.p, v.q, v.cols, v.hdr_on, v.partials, v.counters + 6, \
+  spmm_w<double, W>(k, v.p, v.q, v.cols, v.hdr_on, v.partials, v.counters + 6, \
                     nullptr, true, st)
   ELX_W_DISPATCH(v.w, CALL)
 #undef CALL

@@ -11,8 +11,6 @@
 using elx::DBuf;
 using elx::Error;
 
-constexpr int kFp32Single = 1, kFp32Block = 2;
-
 struct elx_ctx {
   int device = 0;
   int verbose = 0;
@@ -23,22 +21,21 @@ struct elx_ctx {
   elx::Mesh mesh;
   elx::Structure s;
   bool have_mesh = false, have_structure = false, have_matrix = false;
-  // FP32 matrix copies made since the last assembly: kFp32Single (the
-  // single-vector product's: sliced node blocks, or the scalar CSRC arrays),
-  // kFp32Block (block-major node blocks, for the block solver)
-  int have_fp32 = 0;
+  // the FP32 copy of the matrix (sliced node blocks, or the scalar CSRC
+  // arrays) was made since the last assembly
+  bool have_fp32 = false;
 
   // mesh (colour order) and structure
   DBuf conn, mat, elnum, slot, x, eq, e;
   DBuf ia, ja, iat, jat, pt, ja16, jat16;
-  // node blocks (when the numbering allows them): pattern and values
-  DBuf bia, bja, bt, bval, bval32;
-  // the FP32 sliced copy of the node blocks and its pattern; read with
-  // streaming loads unless it fits in 60 % of L2 (ELX_SELL_STREAM=0/1 forces
-  // either: 49.7 against 54.5 us on the 64^3 HEXA8 cube, 277 MB; 17.2
-  // against 12.6 us on the 48^3 TETRA4 mesh, 64 MB)
+  // node blocks (when the numbering allows them): block row pointers and
+  // mirror positions (read by the fill of the sliced copies)
+  DBuf bia, bt;
+  // the sliced copies of the node blocks (FP64, always; FP32 for the mixed
+  // solvers) and their pattern; each read with streaming loads unless it
+  // fits in 60 % of L2
   DBuf sell_ptr, sell_col, sell_val, sell_val64, sell_d16;
-  bool sell_stream = true;
+  bool sell_stream = true, sell64_stream = true;
   bool use_blocks = false;
   // tiled transposed index of the SpMV and its halo slots
   DBuf tile_tgt, tile_out, tgt_col, tgt_start, tpos, halo_ptr, halo_slot, tile_desc, part;
@@ -47,12 +44,7 @@ struct elx_ctx {
   int spmv_kind = elx::kSpmvGather;  // FP64 SpMV kernel family
   bool use_delta = true;             // 16-bit column deltas when the bandwidth fits
   int gather_blocks = 0;             // gather SpMV grid (0: default)
-  // FP32 node-block product: 0 = the sliced kernel, else the lane-group
-  // kernel with this many lanes per block row (16 and 8 measured alike,
-  // 68.8 / 67.9 us on the 64^3 HEXA8 cube and 20.8 us on the 48^3 TETRA4
-  // mesh, against 86.3 / 24.5 us for one thread per row and 80.4 / 31.0 us
-  // for 32 lanes)
-  int group_lanes = 0;
+  int spmm_unroll = 0;  // slot groups in flight in the block product (0: default)
   // state and solver vectors
   DBuf u, b0, b, xs, r, p, q, m, z;
   // mixed precision: FP32 inner PCG vectors and preconditioner
@@ -77,7 +69,7 @@ struct elx_ctx {
   char *vtk_host = nullptr;
   size_t vtk_host_bytes = 0;
   // BiCGSTAB (r0, t) and GMRES (Krylov basis, small dense arrays, state)
-  DBuf r0v, tv, gbasis, garrays, gstate;
+  DBuf r0v, tv, unit, gbasis, garrays, gstate;
   // block PCG: multi-vectors of up to blk_cap columns, scalars, staging
   DBuf bk_b, bk_x, bk_r, bk_p, bk_q, bk_z, bk_xlo, bk_r32, bk_p32, bk_q32, bk_cols, bk_hdr,
       bk_part, bk_cnt, bk_diag, bk_colmajor;
@@ -97,6 +89,7 @@ struct elx_ctx {
   cudaGraphExec_t pcg_graph = nullptr;    // kBatch FP64 PCG iterations
   cudaGraphExec_t pcg32_graph = nullptr;  // kBatch FP32 inner PCG iterations
   cudaGraphExec_t bicg_graph = nullptr;   // kBatch BiCGSTAB iterations
+  bool bicg_plain = false;                // bicg_graph has M = I (no preconditioner)
   cudaGraphExec_t gmres_graph = nullptr;  // one GMRES(gmres_k) restart cycle
   int gmres_k = 0, gmres_launches = 0;
   int pcg_graph_iters = 0;
@@ -165,16 +158,17 @@ struct elx_ctx {
     k.ad = ad.as<double>(); k.al = al.as<double>(); k.alt = alt.as<double>();
     k.ad32 = ad32.as<float>(); k.al32 = al32.as<float>(); k.alt32 = alt32.as<float>();
     k.gather_blocks = gather_blocks;
+    k.max_grid = elx::grid_cap(8);
+    k.spmm_unroll = spmm_unroll;
     if (use_blocks) {
       k.bsize = s.bsize; k.nb = s.nb; k.nnzb = s.nnzb;
-      k.bia = bia.as<int32_t>(); k.bja = bja.as<int32_t>(); k.bt = bt.as<int32_t>();
-      k.bval = bval.as<double>(); k.bval32 = bval32.as<float>();
-      k.group_lanes = group_lanes;
+      k.bia = bia.as<int32_t>(); k.bt = bt.as<int32_t>();
       k.nslices = s.nslices;
       k.sell_ptr = sell_ptr.as<int32_t>(); k.sell_col = sell_col.as<int32_t>();
       k.sell_val = sell_val.as<float>();
       k.sell_stream = sell_stream;
       k.sell_val64 = sell_val64.as<double>();
+      k.sell64_stream = sell64_stream;
       k.sell_d16 = static_cast<const int16_t *>(sell_d16.p);
     }
     return k;
@@ -200,7 +194,6 @@ void upload_structure(elx_ctx *c, bool prederived = false);
 void assemble_resident(elx_ctx *c);
 void build_preconditioner(elx_ctx *c);
 void release_block(elx_ctx *c);
-void ensure_sell64(elx_ctx *c);
 // Row-block partitions on one device (partition.cu).
 void ensure_partitions(elx_ctx *c, int nparts);
 void release_partitions(elx_ctx *c);

@@ -124,6 +124,11 @@ struct Structure {
 
 constexpr int kSliceRows = 32;
 
+// Streaming multiprocessors of the current device (read once per device).
+int sm_count();
+// Grid bound of the grid-stride kernels: per_sm CTAs on every SM.
+inline int grid_cap(int per_sm) { return sm_count() * per_sm; }
+
 // One row-block partition of the CSRC (structure.cpp): owned global
 // equations [eq0, eq0 + neq), local numbering owned 1..neq then the halo
 // (equations outside the block that owned rows couple to, ascending) from
@@ -146,6 +151,7 @@ int32_t number_equations(const Mesh &m, const std::vector<int32_t> &perm,
 void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> &xadj,
                   const std::vector<int32_t> &adj, std::vector<int32_t> &ia,
                   std::vector<int32_t> &ja);
+int color_elements(const Mesh &m, std::vector<int32_t> &color);
 void derive_structure(const Mesh &m, Structure &s);
 void build_tiles(Structure &s, int tile_rows);
 void build_transpose(Structure &s);
@@ -178,22 +184,24 @@ struct CsrcDev {
   double *ad, *al, *alt;
   float *ad32, *al32, *alt32;
   int32_t gather_blocks = 0;  // grid of the gather SpMV (0: default)
-  // node blocks (null bval: none); see Structure
+  // node blocks (bsize 0: none); see Structure
   int32_t bsize = 0, nb = 0;
   int64_t nnzb = 0;
-  const int32_t *bia = nullptr, *bja = nullptr, *bt = nullptr;
-  double *bval = nullptr;
-  float *bval32 = nullptr;
-  // FP32 node-block product: 0 = the sliced kernel (sell_*), else the
-  // lane-group kernel with this many lanes per block row (reads bval32)
-  int32_t group_lanes = 0;
+  const int32_t *bia = nullptr, *bt = nullptr;
   int32_t nslices = 0;
   const int32_t *sell_ptr = nullptr, *sell_col = nullptr;
   float *sell_val = nullptr;
   bool sell_stream = true;  // streaming loads (the copy does not stay in L2)
-  double *sell_val64 = nullptr;  // sliced FP64 copy (null: the FP64 product reads bval)
-  // the FP32 product's columns as 16-bit offsets from the block row (null:
-  // the matrix's block bandwidth does not fit; sell_col is read)
+  double *sell_val64 = nullptr;  // sliced FP64 copy
+  bool sell64_stream = true;     // streaming loads of the FP64 copy
+  // slot groups whose loads the block product issues together (0: default)
+  int32_t spmm_unroll = 0;
+  // grid bound of the products with fused dots: eight CTAs per SM (the
+  // partial sums hold one row per CTA)
+  int32_t max_grid = 1;
+  // the sliced columns as 16-bit offsets from the block row (null: the
+  // matrix's block bandwidth does not fit, or the copies stay in L2;
+  // sell_col is read)
   const int16_t *sell_d16 = nullptr;
 };
 
@@ -262,12 +270,14 @@ void launch_edge_loads(int nnodes, const int32_t *node, const int32_t *ptr, cons
                        int32_t *bad, cudaStream_t st);
 void launch_demote_values(const CsrcDev &k, cudaStream_t st);
 void launch_transpose_values(const CsrcDev &k, cudaStream_t st);
-// Node-block values from the CSRC arrays (k.bval), and their FP32 copy.
-void launch_fill_blocks(const CsrcDev &k, cudaStream_t st);
-void launch_demote_blocks(const CsrcDev &k, cudaStream_t st);
-// FP32 sliced copy of k.bval (k.sell_val), FP64 sliced copy (k.sell_val64)
-void launch_demote_sell(const CsrcDev &k, cudaStream_t st);
-void launch_copy_sell64(const CsrcDev &k, cudaStream_t st);
+// The sliced node-block copies from the CSRC arrays: FP64 (k.sell_val64),
+// FP32 (k.sell_val).
+void launch_fill_sell64(const CsrcDev &k, cudaStream_t st);
+void launch_fill_sell32(const CsrcDev &k, cudaStream_t st);
+// FP64 FMAs per second of the device (a register-only probe kernel, best of
+// five timed launches) and, optionally, per clock per SM at the device's
+// maximum SM clock.
+double measure_fp64_fma_rate(int device, double *per_clock_per_sm);
 // y = K x with the sliced FP64 kernel on explicit arrays (a partition's
 // local slices; no dot product)
 void launch_sell64_local(int nb, int nslices, int bsize, const int32_t *sell_ptr,

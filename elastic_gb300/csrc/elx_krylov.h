@@ -84,7 +84,7 @@ struct BlockVecs {
   ColScalars *cols = nullptr;
   BlockHeader *hdr = nullptr;     // the solve's header
   BlockHeader *hdr_on = nullptr;  // a header with active = 1 (products outside a solve)
-  double *partials = nullptr;     // 2 * 16 * 1216 doubles
+  double *partials = nullptr;     // 2 * 16 * (8 CTAs per SM) doubles
   unsigned int *counters = nullptr;  // 8
 };
 bool block_width_supported(int w);

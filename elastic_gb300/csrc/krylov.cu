@@ -23,6 +23,7 @@
 // (checked every few iterations) it is replaced by the FP64 residual
 // b - K x_hi; the stopping test is the reference's ||r||_M < tol ||b||_M on
 // that FP64 residual.
+#include <atomic>
 #include <cstdlib>
 
 #include "elx_krylov.h"
@@ -442,13 +443,29 @@ void launch_rel_iteration(const CsrcDev &k, const double *b, const double *m, do
   ELX_CUDA(cudaGetLastError());
 }
 
+int sm_count() {
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices];
+  int dev = 0;
+  ELX_CUDA(cudaGetDevice(&dev));
+  const bool cached = dev >= 0 && dev < kMaxDevices;
+  if (cached) {
+    const int v = cache[dev].load(std::memory_order_relaxed);
+    if (v > 0) return v;
+  }
+  int n = 0;
+  ELX_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  if (cached) cache[dev].store(n, std::memory_order_relaxed);
+  return n;
+}
+
 int vector_grid(int n) {
   // a fixed multiple of the SM count keeps the partial count small and fixed;
-  // two blocks per SM (304) beat eight (1216): the last block's sum of the
+  // two blocks per SM beat eight: the last block's sum of the
   // partials is shorter and the streams stay full with grid-stride loops
   // (FP64 PCG 57.6 against 58.9 ms on the 64^3 HEXA8 cube, 121.5 against
-  // 128.9 ms on the 48^3 TETRA4 mesh; 152 / 228 / 456 / 608 / 2432 no better)
-  constexpr int cap = 304;
+  // 128.9 ms on the 48^3 TETRA4 mesh; one, 1.5, 3, 4 and 16 per SM no better)
+  const int cap = grid_cap(2);
   int g = (n + kThreads - 1) / kThreads;
   return g < cap ? (g < 1 ? 1 : g) : cap;
 }

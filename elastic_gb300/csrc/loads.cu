@@ -74,7 +74,7 @@ __global__ void edge_load_kernel(int nnodes, const int32_t *__restrict__ node,
 }
 
 int grid_for(int64_t n) {
-  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 152 * 8));
+  return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, grid_cap(8)));
 }
 
 }  // namespace

@@ -103,13 +103,12 @@ void release_partitions(elx_ctx *c) {
 void partition_product(elx_ctx *c, int nparts, const double *x, double *y) {
   require(c->use_blocks, ELX_ERR_ARG,
           "the partitioned product needs node blocks (every node all free or all fixed)");
-  ensure_sell64(c);
-  require(c->sell_val64.p != nullptr, ELX_ERR_STATE, "the sliced FP64 copy is switched off");
+  require(c->sell_val64.p != nullptr, ELX_ERR_STATE, "sliced FP64 node blocks missing");
   ensure_partitions(c, nparts);
   const int B = c->s.bsize;
   for (const elx_ctx::DevPartition &d : c->parts) {
     const int64_t nown = (int64_t)(d.I1 - d.I0) * B, n = nown + (int64_t)d.nhb * B;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 1216));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, elx::grid_cap(8)));
     elx::partition_gather_kernel<<<grid, 256, 0, c->stream>>>(
         nown, n, B, (int64_t)d.I0 * B, d.hb.as<int32_t>(), x, d.xloc.as<double>());
     ELX_CUDA(cudaGetLastError());

@@ -332,24 +332,24 @@ int64_t estimate_bytes(const SrvRequest &q) {
   int64_t b = 0;
   b += 4 * nen * numel + 8 * numel + 4 * (int64_t)s.slot.size() + 8 * (int64_t)m.x.size() +
        4 * (int64_t)s.id.size() + 8 * (int64_t)m.e.size();
-  b += 4 * (n + 1) + 4 * nad;                          // ia, ja
-  b += 4 * (s.nb + 1) + 8 * s.nnzb;                    // bia, bja, bt
-  b += 8 * s.nnzb * s.bsize * s.bsize;                 // block values
-  b += 8 * n + 8 * nad;                                // ad, al
+  // ia, the node-block pattern (bia, bt), the sliced FP64 copy (values,
+  // columns, 16-bit offsets, pointers), ad, al
+  const int64_t slots = (int64_t)s.sell_ptr[s.nslices] * elx::kSliceRows;
+  b += 4 * (n + 1) + 4 * (s.nb + 1) + 4 * s.nnzb;
+  b += 8 * slots * s.bsize * s.bsize + 6 * slots + 4 * (s.nslices + 1) + 6 * 64;
+  b += 8 * n + 8 * nad;
   b += 8 * (int64_t)(m.ndf * m.nnode) + 8 * 8 * n;     // u, b0, b, x, r, p, q, m, z
   if (q.large) {
     // block PCG of up to 16 columns: b, x in the request's buffer; block
-    // multi-vectors (7 FP64, 4 FP32 per column), FP32 blocks and vectors
+    // multi-vectors (7 FP64, 4 FP32 per column), the sliced FP32 copy and
+    // the FP32 vectors
     int w = 1;
     while (w < q.nrhs && w < 16) w *= 2;
     b += 2 * 8 * n * q.nrhs + 7 * 8 * n * w + 4 * 4 * n * w;
-    b += 4 * s.nnzb * s.bsize * s.bsize + 5 * 4 * n;
-    b += 8 * 2 * 16 * 1216 + (64 << 10);
+    b += 4 * slots * s.bsize * s.bsize + 5 * 4 * n;
+    b += 8 * 2 * 16 * elx::grid_cap(8) + (64 << 10);
   } else {
     b += 5 * 8 * n * q.nrhs;                           // per load case
-    // the sliced FP64 copy of the packed product: values, columns, pointers
-    const int64_t slots = (int64_t)s.sell_ptr[s.nslices] * elx::kSliceRows;
-    b += 8 * slots * s.bsize * s.bsize + 4 * slots + 4 * (s.nslices + 1) + 3 * 64;
   }
   b += 160 << 10;                                      // scalars, partials, padding
   return b;
@@ -466,8 +466,7 @@ void admit(elx_server *sv, SrvRequest &q) {
   const size_t n = (size_t)c->s.neq;
   if (!q.large) {
     // the packed product reads the sliced FP64 copy
-    ensure_sell64(c);
-    require(c->sell_val64.p != nullptr, ELX_ERR_STATE, "the sliced FP64 copy is switched off");
+    require(c->sell_val64.p != nullptr, ELX_ERR_STATE, "sliced FP64 node blocks missing");
   }
   if (q.large) {
     // b and x of all load cases (column-major) for the request's block solve

@@ -42,6 +42,7 @@
 #include "elx_reduce.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdlib>
 
 namespace elx {
@@ -374,14 +375,15 @@ __global__ void permute_kernel(int64_t n, const int32_t *__restrict__ pt,
 int gather_grid(int neq, int lanes) {
   const int rpb = 256 / lanes;
   const int g = (neq + rpb - 1) / rpb;
-  return g < 4864 ? (g < 1 ? 1 : g) : 4864;  // fixed upper bound: 152 SMs x 32
+  const int cap = grid_cap(32);  // fixed upper bound: 32 CTAs per SM
+  return g < cap ? (g < 1 ? 1 : g) : cap;
 }
 
 template <class T, int EPI>
 void launch_gather(const CsrcDev &k, const T *al, const T *alt, const T *ad, const T *x, T *y,
                    const T *w, PcgScalars *sc, double *partials, unsigned int *counter,
                    cudaStream_t st, const int32_t *gate = nullptr) {
-  if (k.bval) {  // node blocks
+  if (k.bsize > 0) {  // node blocks
     launch_bcsr<T, EPI>(k, x, y, w, sc, partials, counter, gate, st);
     return;
   }
@@ -391,7 +393,7 @@ void launch_gather(const CsrcDev &k, const T *al, const T *alt, const T *ad, con
   // CTAs, so that it costs little when the gate is closed
   int grid = gather_grid(k.neq, 4);
   if (k.gather_blocks > 0) grid = std::min(grid, k.gather_blocks);
-  if (gate) grid = std::min(grid, 1216);
+  if (gate) grid = std::min(grid, k.max_grid);
   if (k.ja16)
     gather_spmv_kernel<T, 4, 4, EPI, 0, true><<<grid, 256, 0, st>>>(
         k.neq, k.ia, k.ja, al, k.iat, k.jat, alt, ad, x, y, w, sc, partials, counter, gate,
@@ -465,10 +467,10 @@ void launch_tile_spmv32(const CsrcDev &k, const TileDev &t, const float *x, floa
 
 // FP32 copies of ad, al and alt for the mixed-precision inner iteration.
 void launch_demote_values(const CsrcDev &k, cudaStream_t st) {
-  demote_kernel<<<608, 256, 0, st>>>(k.neq, k.ad, k.ad32);
+  demote_kernel<<<grid_cap(4), 256, 0, st>>>(k.neq, k.ad, k.ad32);
   if (k.nad) {
-    demote_kernel<<<1216, 256, 0, st>>>(k.nad, k.al, k.al32);
-    demote_kernel<<<1216, 256, 0, st>>>(k.nad, k.alt, k.alt32);
+    demote_kernel<<<grid_cap(8), 256, 0, st>>>(k.nad, k.al, k.al32);
+    demote_kernel<<<grid_cap(8), 256, 0, st>>>(k.nad, k.alt, k.alt32);
   }
   ELX_CUDA(cudaGetLastError());
 }
@@ -476,7 +478,7 @@ void launch_demote_values(const CsrcDev &k, cudaStream_t st) {
 // alt = al permuted into column order (after every assembly or upload).
 void launch_transpose_values(const CsrcDev &k, cudaStream_t st) {
   if (k.nad == 0) return;
-  permute_kernel<double><<<1216, 256, 0, st>>>(k.nad, k.pt, k.al, k.alt);
+  permute_kernel<double><<<grid_cap(8), 256, 0, st>>>(k.nad, k.pt, k.al, k.alt);
   ELX_CUDA(cudaGetLastError());
 }
 
@@ -560,9 +562,11 @@ struct NoAllocScratch {
 
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
-// Device address of the scratch per device, looked up once per device.
+// Device address of the scratch per device (in the device's primary
+// context), looked up once per device.  Two host threads making their first
+// call on one device at once both look it up and store the same address.
 constexpr int kMaxDevices = 64;
-NoAllocScratch *g_noalloc_addr[kMaxDevices] = {nullptr};
+std::atomic<NoAllocScratch *> g_noalloc_addr[kMaxDevices];
 
 }  // namespace
 }  // namespace elx
@@ -576,16 +580,18 @@ extern "C" int elx_spmv_dot_noalloc(int32_t neq, const int32_t *ia, const int32_
   if (!ia || !ja || !ad || !al || !iat || !jat || !alt || !x || !y || !xy) return ELX_ERR_ARG;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return ELX_ERR_CUDA;
-  if (!g_noalloc_addr[dev]) {
+  NoAllocScratch *sc = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (!sc) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return ELX_ERR_CUDA;
-    g_noalloc_addr[dev] = static_cast<NoAllocScratch *>(p);
+    sc = static_cast<NoAllocScratch *>(p);
+    g_noalloc_addr[dev].store(sc, std::memory_order_release);
   }
-  NoAllocScratch *sc = g_noalloc_addr[dev];
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // the ticket and the scalars must start at zero (done = 0 lets the kernel run)
-  if (cudaMemsetAsync(&sc->scalars, 0, sizeof(PcgScalars) + sizeof(unsigned int), st) !=
-      cudaSuccess)
+  // the scalars and the ticket must start at zero (done = 0 lets the kernel
+  // run; the ticket counts the blocks that have published their partials)
+  if (cudaMemsetAsync(&sc->scalars, 0, sizeof(PcgScalars), st) != cudaSuccess ||
+      cudaMemsetAsync(&sc->counter, 0, sizeof(unsigned int), st) != cudaSuccess)
     return ELX_ERR_CUDA;
   const int grid = (neq + kNoAllocRowsPerBlock - 1) / kNoAllocRowsPerBlock;
   gather_spmv_kernel<double, 4, 4, kEpiPcg, 1><<<grid, 256, 0, st>>>(

@@ -320,7 +320,7 @@ __global__ void update_kernel(int64_t n, const int32_t *__restrict__ eq,
 }  // namespace
 
 void launch_update(int64_t n, const int32_t *eq, const double *x, double *u, cudaStream_t st) {
-  const int grid = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, grid_cap(8));
   update_kernel<<<std::max(grid, 1), 256, 0, st>>>(n, eq, x, u);
   ELX_CUDA(cudaGetLastError());
 }
@@ -357,7 +357,7 @@ void launch_stress(const MeshDev &m, const Segment &seg, const double *u, double
 void launch_stress_average(int nnode, int ntn, const int32_t *count, const double *tx0,
                            double *ts, cudaStream_t st) {
   const int64_t n = (int64_t)nnode * ntn;
-  const int grid = (int)std::min<int64_t>((n + 255) / 256, 152 * 8);
+  const int grid = (int)std::min<int64_t>((n + 255) / 256, grid_cap(8));
   stress_average_kernel<<<std::max(grid, 1), 256, 0, st>>>(nnode, ntn, count, tx0, ts);
   ELX_CUDA(cudaGetLastError());
 }

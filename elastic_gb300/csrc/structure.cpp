@@ -267,18 +267,15 @@ void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> 
   }
 }
 
-// What the assembly kernels need beyond ia/ja/id:
-//  * a greedy element colouring in which no two elements of a colour share a
-//    node (so colour-ordered assembly needs no atomics), elements grouped per
-//    colour and element type;
-//  * the slot map: for each element and each unordered pair of its nodes
-//    {a, b} with free dofs, the offset within the row of the higher node of
-//    the lower node's first column (identical for every dof row of that node).
-// The SpMV's tiled transposed index is built by build_tiles.
-void derive_structure(const Mesh &m, Structure &s) {
-  // ---- element colouring
+// Greedy element colouring: each element, in element order, takes the
+// smallest colour none of its vertex nodes has yet, so that the elements of
+// one colour share no node (and so no equation): the assembly kernels then
+// add element blocks colour by colour without atomics.  Any colouring with
+// that property serves (the reference's colormsh, Colormsh.f:9-308, is
+// another); returns the number of colours, color[el] 0-based.
+int color_elements(const Mesh &m, std::vector<int32_t> &color) {
   const int nen1 = m.nen + 1;
-  std::vector<int32_t> color(m.numel, -1);
+  color.assign(m.numel, -1);
   std::vector<std::vector<uint64_t>> used;  // per node, bit per colour (64 per word)
   int words = 1;
   used.assign(m.nnode, std::vector<uint64_t>(words, 0));
@@ -301,7 +298,22 @@ void derive_structure(const Mesh &m, Structure &s) {
     ncolors = std::max(ncolors, chosen + 1);
     for (int a = 0; a < nv; a++) used[c[a] - 1][chosen / 64] |= 1ull << (chosen % 64);
   }
-  s.ncolors = ncolors;
+  return ncolors;
+}
+
+// What the assembly kernels need beyond ia/ja/id:
+//  * a greedy element colouring in which no two elements of a colour share a
+//    node (so colour-ordered assembly needs no atomics), elements grouped per
+//    colour and element type;
+//  * the slot map: for each element and each unordered pair of its nodes
+//    {a, b} with free dofs, the offset within the row of the higher node of
+//    the lower node's first column (identical for every dof row of that node).
+// The SpMV's tiled transposed index is built by build_tiles.
+void derive_structure(const Mesh &m, Structure &s) {
+  // ---- element colouring
+  const int nen1 = m.nen + 1;
+  std::vector<int32_t> color;
+  s.ncolors = color_elements(m, color);
   // group by (colour, element type), elements ascending inside a group
   s.elem_order.resize(m.numel);
   std::iota(s.elem_order.begin(), s.elem_order.end(), 0);

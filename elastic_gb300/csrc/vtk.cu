@@ -507,7 +507,7 @@ void launch_vtk(const VtkLayout &L, char *dbuf, const MeshDev &m, int ntn, int n
     ELX_CUDA(cudaMemcpyAsync(dbuf + t.off, t.s.data(), t.s.size(), cudaMemcpyHostToDevice, st));
   for (const VtkLayout::Section &s : L.sections) {
     if (s.count <= 0) continue;
-    const int grid = std::max(1, std::min((s.count + 255) / 256, 152 * 8));
+    const int grid = std::max(1, std::min((s.count + 255) / 256, grid_cap(8)));
     vtk_section_kernel<<<grid, 256, 0, st>>>(A, Sec{s.kind, s.off}, s.count);
     ELX_CUDA(cudaGetLastError());
   }
@@ -516,7 +516,7 @@ void launch_vtk(const VtkLayout &L, char *dbuf, const MeshDev &m, int ntn, int n
 
 void launch_fortran_e(const double *x, int n, int w, int d, int e, char *out, cudaStream_t st) {
   if (n <= 0) return;
-  fortran_e_kernel<<<std::max(1, std::min((n + 255) / 256, 1216)), 256, 0, st>>>(x, n, w, d, e,
+  fortran_e_kernel<<<std::max(1, std::min((n + 255) / 256, grid_cap(8))), 256, 0, st>>>(x, n, w, d, e,
                                                                                  out);
   ELX_CUDA(cudaGetLastError());
 }

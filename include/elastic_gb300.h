@@ -54,6 +54,10 @@ extern "C" {
 #define ELX_SOLVER_PCG 1
 #define ELX_SOLVER_GMRES 2
 #define ELX_SOLVER_BICGSTAB 4
+/* BiCGSTAB without a preconditioner (bicgstab, Iters.f:812-1075): the
+ * reference has no solver code for it (its only call is commented out at
+ * Solv.f:334); stops on ||r|| < tol ||b||; info->norm_m_r = ||b - K x||. */
+#define ELX_SOLVER_BICGSTAB_NOPREC 5
 
 /* precision of the Krylov iteration */
 #define ELX_PREC_FP64 0  /* everything in FP64, as the reference          */
@@ -135,6 +139,12 @@ int elx_host_structure_sizes(const elx_host_structure *h, int32_t *neq,
                              int64_t *nad);
 int elx_host_structure_get(const elx_host_structure *h, int32_t *perm,
                            int32_t *id, int32_t *ia, int32_t *ja);
+/* The element colours the assembly kernels use (in place of colormsh's
+ * elcolor, Colormsh.f:9-308: elements of one colour share no node, so their
+ * blocks are added without atomics): elcolor(numel) 1-based colours
+ * (nullable), *ncolors their number (nullable). */
+int elx_host_structure_colors(const elx_host_structure *h, int32_t *elcolor,
+                              int32_t *ncolors);
 void elx_host_structure_destroy(elx_host_structure *h);
 
 /* Row-block partitions for a multi-GPU run (one partition per GPU), in the
@@ -340,6 +350,14 @@ int elx_partition_spmv_resident(elx_ctx *ctx, int32_t nparts, int32_t reps);
 int elx_partition_info(elx_ctx *ctx, int32_t nparts, int32_t part, int32_t *eq0,
                        int32_t *neq, int32_t *nhalo);
 
+/* The FP64 pipe's rate on `device`, measured: FMAs per second of a
+ * register-only probe kernel (eight independent FMA chains per thread, one
+ * resident wave, best of five timed launches) and, if per_clock_per_sm is
+ * not NULL, that rate per clock per SM at the device's maximum SM clock.
+ * No reference counterpart: the FP64 product's floor (one FMA per stored
+ * entry of the full matrix) is this rate. */
+int elx_fp64_fma_rate(int32_t device, double *fma_per_s, double *per_clock_per_sm);
+
 /* Test hook of the device number formatter: n fields Ew.d (e = 0) or
  * Ew.dEe of x into out (n * w chars), as the writer prints them. */
 int elx_fortran_e(const double *x, int32_t n, int32_t w, int32_t d, int32_t e, char *out);
@@ -364,7 +382,9 @@ int elx_fortran_e(const double *x, int32_t n, int32_t w, int32_t d, int32_t e, c
  * 130 KB) is a static device array that every GPU loading this library
  * holds until the process exits.  The first call on a device looks up that
  * array's device address (with the device current): make that first call
- * before any stream capture.  All calls share the scratch, so calls that
+ * before any stream capture.  The address is that of the device's primary
+ * context (the CUDA runtime's): a caller that makes its own driver-API
+ * context current must not call this entry point from it.  All calls share the scratch, so calls that
  * overlap on the GPU race; serialise them on one stream.  Returns ELX_OK
  * once the work is enqueued on `stream`. */
 int elx_spmv_dot_noalloc(int32_t neq, const int32_t *ia, const int32_t *ja,

@@ -100,6 +100,7 @@ def lib():
         sol = [C.c_int, C.c_longlong, I32P, I32P, F64P, F64P, F64P, F64P]
         L.orc_pcg.argtypes = sol + [C.c_double, C.c_int, C.POINTER(Info)]
         L.orc_pbicgstab.argtypes = sol + [C.c_double, C.c_int, C.POINTER(Info)]
+        L.orc_bicgstab.argtypes = sol + [C.c_double, C.c_int, C.POINTER(Info)]
         L.orc_gmres.argtypes = sol + [C.c_int, C.c_double, C.c_int, C.POINTER(Info)]
         L.orc_pcg_omp.argtypes = sol + [C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(Info)]
         L.orc_matvec_csrcsym_omp.argtypes = [C.c_int, I32P, I32P, F64P, F64P, F64P, F64P, C.c_int,
@@ -351,6 +352,16 @@ def pcg_omp(s, ad, al, b, tol=1e-11, maxit=10000, nthreads=None, stop_at_maxit=F
 def pbicgstab(s, ad, al, b, tol=1e-11, maxit=10000):
     """pbicgstab (Iters.f:1079-1349)."""
     return _solve(lib().orc_pbicgstab, s, ad, al, b, tol, maxit)
+
+
+def flop_cg(neq, nad, iters):
+    """flop_cg (Matvec.f:1499-1531): the PCG's floating-point operations."""
+    return lib().orc_flop_cg(int(neq), int(nad), int(iters))
+
+
+def bicgstab(s, ad, al, b, tol=1e-11, maxit=10000):
+    """bicgstab (Iters.f:812-1075): no preconditioner, beta from (r, b)."""
+    return _solve(lib().orc_bicgstab, s, ad, al, b, tol, maxit)
 
 
 def gmres(s, ad, al, b, k=50, tol=1e-11, maxit=10000):

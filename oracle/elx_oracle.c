@@ -1554,6 +1554,78 @@ int orc_pbicgstab(int neq, long long nad, const int *ia, const int *ja,
   return status;
 }
 
+/* Iters.f:812-1075 bicgstab: BiCGSTAB without a preconditioner, x0 = 0
+ * (fnew), stopping on the 2-norm, sqrt|(r, r)| < tol sqrt|(b, b)|, after
+ * each half step.  Its beta takes (r, b) where the method has (r, r0)
+ * (Iters.f:987); with x0 = 0, r0 = b - K 0 = b exactly, so the two agree.
+ * Unreachable from the reference's decks (its only call is commented out,
+ * Solv.f:334); norm_m_r is reported as ||b - K x|| (no M). */
+int orc_bicgstab(int neq, long long nad, const int *ia, const int *ja,
+                 const double *ad, const double *al, const double *b,
+                 double *x, double tol, int maxit, orc_info *info) {
+  double t0 = wall();
+  (void)nad;
+  for (int i = 0; i < neq; i++)
+    if (ad[i] == 0.0) { if (info) info->status = ORC_ERR_ZERO_DIAG; return ORC_ERR_ZERO_DIAG; }
+  size_t sz = (size_t)neq * sizeof(double);
+  double *t = malloc(sz), *v = malloc(sz), *r = malloc(sz), *p = malloc(sz), *r0 = malloc(sz);
+  if (!t || !v || !r || !p || !r0) {
+    free(t); free(v); free(r); free(p); free(r0);
+    return ORC_ERR_OOM;
+  }
+  for (int i = 0; i < neq; i++) x[i] = 0.0;
+  double d = orc_dot(b, b, neq);
+  double conv = tol * sqrt(fabs(d));
+  orc_matvec_csrcsym1(neq, ia, ja, ad, al, x, p);
+  for (int i = 0; i < neq; i++) {
+    r0[i] = b[i] - p[i];
+    r[i] = r0[i];
+    p[i] = r0[i];
+  }
+  int j, converged = 0;
+  for (j = 1; j <= maxit; j++) {
+    orc_matvec_csrcsym1(neq, ia, ja, ad, al, p, v);
+    double rr0 = orc_dot(r, r0, neq);
+    double alpha = rr0 / orc_dot(v, r0, neq);
+    for (int i = 0; i < neq; i++) {
+      x[i] = x[i] + alpha * p[i];
+      r[i] = r[i] - alpha * v[i];
+    }
+    d = orc_dot(r, r, neq);
+    if (sqrt(fabs(d)) < conv) { converged = 1; break; }
+    orc_matvec_csrcsym1(neq, ia, ja, ad, al, r, t);
+    double w = orc_dot(t, r, neq) / orc_dot(t, t, neq);
+    for (int i = 0; i < neq; i++) {
+      x[i] = x[i] + w * r[i];
+      r[i] = r[i] - w * t[i];
+    }
+    d = orc_dot(r, r, neq);
+    if (sqrt(fabs(d)) < conv) { converged = 1; break; }
+    double beta = (orc_dot(r, b, neq) / rr0) * (alpha / w);
+    for (int i = 0; i < neq; i++) p[i] = r[i] + beta * (p[i] - w * v[i]);
+  }
+  int status = ORC_OK;
+  if (!converged) { status = ORC_ERR_NO_CONVERGENCE; j = maxit; }
+  orc_matvec_csrcsym1(neq, ia, ja, ad, al, x, p);
+  double xkx = orc_dot(x, p, neq);
+  double norm = sqrt(orc_dot(x, x, neq));
+  for (int i = 0; i < neq; i++) r[i] = b[i] - p[i];
+  double norm_r = sqrt(orc_dot(r, r, neq));
+  if (info) {
+    info->iters = j;
+    info->status = status;
+    info->xkx = xkx;
+    info->norm_x = norm;
+    info->norm_r = norm_r;
+    info->norm_m_r = norm_r;
+    info->conv = conv;
+    info->seconds = wall() - t0;
+    info->mflops = 0.0;
+  }
+  free(t); free(v); free(r); free(p); free(r0);
+  return status;
+}
+
 /* Iters.f:528-808 gmres: left-Jacobi GMRES(k), modified Gram-Schmidt,
  * Givens rotations; maxit counts restart cycles; iters = total inner steps. */
 int orc_gmres(int neq, long long nad, const int *ia, const int *ja,

@@ -1,8 +1,9 @@
 """Generates the golden fixtures in this directory from the reference's own
 example decks (lmn-labest/Elastic, input/) and the CPU oracle.
 
-Run in a checkout that has the reference next to it:
-    python tests/golden/make_golden.py /root/reference
+Run with the reference project's checkout as the argument (or in the
+ELASTIC_REFERENCE environment variable):
+    python tests/golden/make_golden.py <path to lmn-labest/Elastic>
 
 It writes
   decks.npz     the 3-D HEXA8 / TETRA4 deck meshes (caso_a, nodal forces), in
@@ -221,4 +222,7 @@ def load_deck_mesh(key):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ELASTIC_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference checkout> (or set ELASTIC_REFERENCE)")
+    main(ref)

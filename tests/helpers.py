@@ -52,10 +52,14 @@ def row_scaled_error(ia, a_ref, a_got, ad_ref, ad_got):
     """max |delta| over the entries of each row, divided by the row's largest
     |entry| (diagonal included): the assembly parity metric."""
     n = ia.shape[0] - 1
-    rows = np.repeat(np.arange(n), np.diff(ia))
+    lens = np.diff(ia)
+    rows = np.repeat(np.arange(n), lens)
     rowmax = np.abs(ad_ref).copy()
     if a_ref.size:
-        np.maximum.at(rowmax, rows, np.abs(a_ref))
+        # rows are contiguous runs of al: the max of each non-empty run
+        full = lens > 0
+        runmax = np.maximum.reduceat(np.abs(a_ref), np.asarray(ia[:-1])[full] - 1)
+        rowmax[full] = np.maximum(rowmax[full], runmax)
     err = np.abs(ad_ref - ad_got) / rowmax
     if a_ref.size:
         err_l = np.abs(a_ref - a_got) / rowmax[rows]

@@ -66,7 +66,7 @@ def test_profiled_figures_come_from_the_committed_summary():
     pipe = bench.profiled("fp64_pipe_frac")
     assert traffic is not None and 4.0e8 < traffic < 1.0e9  # DRAM bytes of one FP64 product
     assert pipe is not None and 0.0 < pipe <= 1.0
-    assert bench.profiled("traffic_bytes_per_launch", "spmm_fp32_w16_hexa8_plate96.md") > 0
+    assert bench.profiled("traffic_bytes_per_launch", "sell_spmm_fp32_w16_hexa8_plate96.md") > 0
     assert bench.profiled("no_such_key") is None
     assert bench.profiled("traffic_bytes_per_launch", "no_such_file.md") is None
 

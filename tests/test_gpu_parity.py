@@ -251,14 +251,13 @@ def test_fp32_spmv_parity(gpu_ctx, name):
     assert rel_inf(y_o, y_g) <= FP32_SPMV_TOL
 
 
-@pytest.mark.parametrize("env", [{"ELX_GROUP_LANES": "16"}, {"ELX_SELL_STREAM": "0"},
+@pytest.mark.parametrize("env", [{"ELX_SELL_STREAM": "0"},
                                  {"ELX_SELL_STREAM": "1"},
                                  {"ELX_SELL_STREAM": "1", "ELX_SELL_D16": "0"}])
 @pytest.mark.parametrize("name", ["quad4_stress", "hexa8"])
 def test_fp32_spmv_kernel_choices(built_lib, monkeypatch, name, env):
     """Each FP32 node-block product (sliced copy with streaming loads and
-    16-bit or 32-bit columns, or cached loads; lane groups on the block-major
-    copy) against the FP64 oracle."""
+    16-bit or 32-bit columns, or cached loads) against the FP64 oracle."""
     for k, v in env.items():
         monkeypatch.setenv(k, v)
     m = MESHES[name]()

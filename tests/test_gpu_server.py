@@ -1,11 +1,11 @@
 """Solve server (elx_server_*): continuous batching of many meshes.
 
 Bars: every load case of every request equals the oracle's FP64 PCG solution
-(pcg, Iters.f:252-524, tol 1e-10) within 1e-9 relative with iterations within
+(pcg, Iters.f:252-524, tol 1e-10) within 1e-10 relative with iterations within
 +-2; a request's result is bitwise the same alone and in a mix; admission
 respects the HBM budget; a bad request fails alone without stopping the
 server; requests above the size threshold, solved whole by the block PCG,
-meet the same bars (FP64 block PCG: 1e-9; mixed: the FP64 stopping test and
+meet the same bars (FP64 block PCG: 1e-10; mixed: the FP64 stopping test and
 1e-6 of the oracle) and are bitwise the same alone and in a mix.
 """
 import numpy as np
@@ -53,7 +53,7 @@ def test_mix_matches_oracle_and_solo(built_lib):
             for k in range(F.shape[0]):
                 assert infos[k]["status"] == 0
                 assert abs(infos[k]["iters"] - it_o[k]) <= 2, (m.name, k)
-                assert rel_inf(U_o[k], U[k]) <= 1e-9, (m.name, k)
+                assert rel_inf(U_o[k], U[k]) <= 1e-10, (m.name, k)
         # the same requests one at a time: bitwise the same results
         for (m, F), (U, infos, _, _) in zip(reqs[:4], mixed[:4]):
             U1, infos1, _, st1 = srv.wait(srv.submit(m, F, tol=TOL, maxit=50000), timeout=300)
@@ -102,7 +102,7 @@ def test_no_convergence_reported(built_lib):
         assert np.isfinite(U).all()
 
 
-@pytest.mark.parametrize("mode,bar", [(2, 1e-6), (1, 1e-9)])
+@pytest.mark.parametrize("mode,bar", [(2, 1e-6), (1, 1e-10)])
 def test_large_requests_solved_whole(built_lib, mode, bar):
     reqs = _requests(11, 6)
     with E.Server(device=0, large_dofs=1, large_mode=mode) as srv:

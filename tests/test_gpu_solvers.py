@@ -1,5 +1,7 @@
-"""GPU BiCGSTAB (pbicgstab, Iters.f:1079-1349) and GMRES(k) (gmres,
-Iters.f:528-808) through the C ABI against the oracle's restatements.
+"""GPU BiCGSTAB (pbicgstab, Iters.f:1079-1349; bicgstab without a
+preconditioner, Iters.f:812-1075) and GMRES(k) (gmres, Iters.f:528-808)
+through the C ABI against the oracle's restatements, and the PCG's flop
+count (flop_cg, Matvec.f:1499-1531).
 
 Unlike CG, neither method's iteration count is stable under rounding.
 BiCGSTAB's residual is not monotone, and restarted GMRES stagnates for
@@ -81,6 +83,58 @@ def test_bicgstab_first_iterates_match(gpu_ctx, name):
         assert i_o["status"] == E.ERR_NO_CONVERGENCE and i_g["status"] == E.ERR_NO_CONVERGENCE
         assert i_g["iters"] == i_o["iters"] == maxit
         assert rel_inf(x_o, x_g) <= FIRST_TOL, maxit
+
+
+# bicgstab (Iters.f:812-1075) without a preconditioner: held at tol 1e-12,
+# where the oracle's own solutions, rerun with b perturbed by one ulp in
+# random entries, spread by at most 1.0e-9 (quad4_stress; 2e-11 on the 3-D
+# meshes) and its iteration counts by -4 / +8 % (e.g. 329-341 against 333).
+@pytest.mark.parametrize("name", sorted(MESHES))
+def test_bicgstab_noprec_parity(gpu_ctx, name):
+    s, ad, al, b = _system(gpu_ctx, name)
+    x_o, i_o = O.bicgstab(s, ad, al, b, tol=1e-12, maxit=20000)
+    x_g, i_g = gpu_ctx.solve(b, solver=E.SOLVER_BICGSTAB_NOPREC, tol=1e-12, maxit=20000)
+    _close_at_convergence(i_o, i_g, x_o, x_g)
+    # no M: the reported M-norm residual is the 2-norm one, as in the oracle
+    assert i_g["norm_m_r"] == i_g["norm_r"]
+    assert i_g["norm_r"] <= 3.16 * i_g["conv"]
+
+
+@pytest.mark.parametrize("name", sorted(MESHES))
+def test_bicgstab_noprec_first_iterates_match(gpu_ctx, name):
+    s, ad, al, b = _system(gpu_ctx, name)
+    for maxit in (1, 6):
+        x_o, i_o = O.bicgstab(s, ad, al, b, tol=1e-14, maxit=maxit)
+        x_g, i_g = gpu_ctx.solve(b, solver=E.SOLVER_BICGSTAB_NOPREC, tol=1e-14, maxit=maxit,
+                                 raise_on_error=False)
+        assert i_o["status"] == E.ERR_NO_CONVERGENCE and i_g["status"] == E.ERR_NO_CONVERGENCE
+        assert i_g["iters"] == i_o["iters"] == maxit
+        assert rel_inf(x_o, x_g) <= FIRST_TOL, maxit
+
+
+def test_bicgstab_then_noprec_then_bicgstab(gpu_ctx):
+    """The preconditioned and the plain solver alternate on one context (each
+    captured graph belongs to one of them)."""
+    s, ad, al, b = _system(gpu_ctx, "hexa8")
+    for solver, ref in ((E.SOLVER_BICGSTAB, O.pbicgstab), (E.SOLVER_BICGSTAB_NOPREC, O.bicgstab),
+                        (E.SOLVER_BICGSTAB, O.pbicgstab)):
+        x_o, _ = ref(s, ad, al, b, tol=1e-14, maxit=3)
+        x_g, _ = gpu_ctx.solve(b, solver=solver, tol=1e-14, maxit=3, raise_on_error=False)
+        assert rel_inf(x_o, x_g) <= FIRST_TOL
+
+
+@pytest.mark.parametrize("name", ["quad4_stress", "hexa8"])
+def test_pcg_flop_count(gpu_ctx, name):
+    """The reported Mflops are flop_cg's count (Matvec.f:1499-1531) over the
+    solve's time: mflops * seconds = the oracle's flop_cg(neq, nad, iters)."""
+    s, ad, al, b = _system(gpu_ctx, name)
+    _, i_g = gpu_ctx.solve(b, tol=1e-10, maxit=20000)
+    _, i_o = O.pcg(s, ad, al, b, tol=1e-10, maxit=20000)
+    flops = O.flop_cg(s.neq, s.nad, i_g["iters"])
+    assert flops == (s.neq + 4 * s.nad + 2 * (2 * s.neq) + 7 * s.neq + 2) * i_g["iters"]
+    np.testing.assert_allclose(i_g["mflops"] * i_g["seconds"] * 1e6, flops, rtol=1e-9)
+    np.testing.assert_allclose(i_o["mflops"] * i_o["seconds"] * 1e6,
+                               O.flop_cg(s.neq, s.nad, i_o["iters"]), rtol=1e-9)
 
 
 # GMRES(7) stagnates on the 2-D meshes (tens of thousands of steps).

@@ -70,10 +70,19 @@ def test_deck_meshes_match_golden_checksums():
         assert sha(sp.ia) == g["ia_sha"] and sha(sp.ja) == g["ja_sha"]
 
 
+@pytest.mark.parametrize("name", ["cube_hexa8_64", "cube_tetra4_48_mixed", "plate_hexa8_96"])
+def test_full_size_structures_bit_exact(name):
+    """The benchmark meshes at full size (811,200 / 345,744 / 1,354,896
+    equations): perm, id, ia, ja bit for bit against the oracle."""
+    m = getattr(M, name)()
+    if isinstance(m, tuple):
+        m = m[0]
+    _same(m, True)
+
+
 def test_full_size_cube_structure_properties():
-    """64^3 HEXA8 (811,200 equations): the structure at full size, checked by
-    size-independent properties (sizes, sorted strictly-lower rows, RCM a
-    permutation) -- the oracle's O(row^2) sort would take minutes here."""
+    """64^3 HEXA8 (811,200 equations): sizes, sorted strictly-lower rows,
+    RCM a permutation."""
     m = M.cube_hexa8_64()
     sp = E.host_structure(m, True)
     assert (sp.neq, sp.nad) == (811200, 31442295)
@@ -82,3 +91,59 @@ def test_full_size_cube_structure_properties():
     assert np.all(sp.ja < rows)
     same_row = rows[1:] == rows[:-1]
     assert np.all(sp.ja[1:][same_row] > sp.ja[:-1][same_row])
+
+
+def colouring_conflicts(mesh, color):
+    """Pairs (colour, node) where two elements of one colour share a vertex
+    node -- and so an equation, whose entries two threads of one assembly
+    launch would then add at once.  The reference's guarantee for its own
+    colouring (Colormsh.f:160-247) restated as a check; 0 means race-free."""
+    nen1 = mesh.nen + 1
+    ix = mesh.ix.reshape(mesh.numel, nen1)
+    nv = np.array([M.NEN_OF_TYPE[int(mesh.ie[ix[el, -1] - 1])]
+                   for el in range(mesh.numel)])
+    seen = {}
+    conflicts = 0
+    for el in range(mesh.numel):
+        for node in ix[el, :nv[el]]:
+            key = (int(color[el]), int(node))
+            if key in seen:
+                conflicts += 1
+            seen[key] = el
+    return conflicts
+
+
+COLOUR_MESHES = dict(MESHES, cube_hexa8_24=lambda: M.box_hexa8(24, 24, 24),
+                     tetra4_cube=lambda: M.box_tetra4(10, 9, 8, jitter=0.2, seed=3))
+
+
+@pytest.mark.parametrize("name", sorted(COLOUR_MESHES))
+def test_element_colouring_is_race_free(name):
+    """No two elements of one colour share a node, every element has a
+    colour, and the colours are 1..ncolors."""
+    m = COLOUR_MESHES[name]()
+    col = E.host_colors(m)
+    assert col.min() == 1 and set(np.unique(col)) == set(range(1, col.max() + 1))
+    assert colouring_conflicts(m, col) == 0
+
+
+def test_element_colouring_full_size_cube():
+    """The 64^3 HEXA8 cube (262,144 elements): race-free, with the greedy
+    colouring's 8 colours of a structured hexahedral mesh, checked with
+    array operations (each colour's vertex nodes all distinct)."""
+    m = M.cube_hexa8_64()
+    col = E.host_colors(m)
+    ix = m.ix.reshape(m.numel, m.nen + 1)[:, :8]
+    assert col.max() == 8
+    for c in range(1, col.max() + 1):
+        nodes = ix[col == c].ravel()
+        assert np.unique(nodes).size == nodes.size, c
+
+
+def test_colouring_check_catches_a_shared_node():
+    """The check itself: two neighbouring elements put in one colour are
+    reported (a mistake planted in a copy of the colours)."""
+    m = M.box_hexa8(4, 3, 3)
+    col = E.host_colors(m).copy()
+    col[1] = col[0]  # elements 0 and 1 share a face
+    assert colouring_conflicts(m, col) > 0

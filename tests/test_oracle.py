@@ -192,7 +192,7 @@ def test_rcm_reduces_bandwidth_of_a_scrambled_numbering():
     assert bw[1] * 3 < bw[0]
 
 
-@pytest.mark.parametrize("solver", ["pcg", "bicgstab", "gmres"])
+@pytest.mark.parametrize("solver", ["pcg", "bicgstab", "bicgstab_noprec", "gmres"])
 def test_solvers_match_direct_solve(solver):
     m = M.box_tetra4(4, 3, 3, jitter=0.2, lognormal_E=True, seed=3)
     s = O.structure(m)
@@ -200,10 +200,48 @@ def test_solvers_match_direct_solve(solver):
     ad, al, b = O.assemble(m, s, u0, b0)
     K = full_matrix(s, ad, al)
     xd = spla.spsolve(K.tocsc(), b)
-    fn = {"pcg": O.pcg, "bicgstab": O.pbicgstab, "gmres": O.gmres}[solver]
+    fn = {"pcg": O.pcg, "bicgstab": O.pbicgstab, "bicgstab_noprec": O.bicgstab,
+          "gmres": O.gmres}[solver]
     x, info = fn(s, ad, al, b, tol=1e-12)
     assert info["status"] == 0
     assert np.abs(x - xd).max() <= 1e-8 * np.abs(xd).max()
+
+
+def test_plain_bicgstab_is_pbicgstab_with_unit_diagonal():
+    """bicgstab (Iters.f:812-1075) is pbicgstab (Iters.f:1079-1349) with
+    M = I, its beta from (r, b) the same as (r, r0) since x0 = 0 gives r0 = b
+    exactly: on a matrix scaled to a unit diagonal (Jacobi M = I) the two
+    restatements agree bitwise, iterate for iterate."""
+    m = M.box_hexa8(5, 4, 4, jitter=0.2, seed=2)
+    m.f = np.random.default_rng(4).standard_normal(m.f.shape) * (m.id == 0)
+    s = O.structure(m)
+    b0, u0 = O.loads(m, s)
+    ad, al, b = O.assemble(m, s, u0, b0)
+    # D^-1/2 K D^-1/2 (D = diag(ad)): its diagonal is one, set exactly
+    rows = np.repeat(np.arange(s.neq), np.diff(s.ia))
+    al1 = al / np.sqrt(ad[rows] * ad[s.ja - 1])
+    ad1 = np.ones(s.neq)
+    for maxit in (1, 5, 40):
+        x1, i1 = O.bicgstab(s, ad1, al1, b, tol=1e-14, maxit=maxit)
+        x2, i2 = O.pbicgstab(s, ad1, al1, b, tol=1e-14, maxit=maxit)
+        assert np.array_equal(x1, x2) and i1["iters"] == i2["iters"] == maxit
+    x1, i1 = O.bicgstab(s, ad, al, b, tol=1e-12)
+    assert i1["status"] == 0 and i1["norm_m_r"] == i1["norm_r"]
+    assert i1["norm_r"] <= 3.16 * i1["conv"]
+
+
+def test_flop_cg_count():
+    """flop_cg (Matvec.f:1499-1531): per iteration one CSRC product
+    (neq + 4 nad, flop_csrc), two dots (2 neq each), 7 neq of vector updates
+    and 2 scalar operations; the PCG's Mflops are that count over its time."""
+    assert O.flop_cg(10, 20, 3) == (10 + 80 + 40 + 70 + 2) * 3
+    m = M.box_hexa8(5, 4, 3)
+    s = O.structure(m)
+    b0, u0 = O.loads(m, s)
+    ad, al, b = O.assemble(m, s, u0, b0)
+    _, info = O.pcg(s, ad, al, b, tol=1e-10)
+    np.testing.assert_allclose(info["mflops"] * info["seconds"] * 1e6,
+                               O.flop_cg(s.neq, s.nad, info["iters"]), rtol=1e-9)
 
 
 def test_openmp_pcg_matches_sequential_pcg():

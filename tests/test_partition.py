@@ -98,6 +98,19 @@ def test_too_many_partitions_refused():
     assert e.value.code == E.ERR_ARG
 
 
+def _join_all(procs, timeout):
+    """Joins the rank processes; a rank still running after `timeout` (hung
+    in a collective) is terminated, so that it holds no port afterwards."""
+    for pr in procs:
+        pr.join(timeout)
+    alive = [pr for pr in procs if pr.is_alive()]
+    for pr in alive:
+        pr.terminate()
+        pr.join(5)
+    assert not alive, "a rank did not finish"
+    assert all(pr.exitcode == 0 for pr in procs), [pr.exitcode for pr in procs]
+
+
 def _rank(rank, world, port, name, q):
     import torch
     import torch.distributed as dist
@@ -141,9 +154,7 @@ def test_two_gloo_ranks_exchange_halos(name):
     procs = [ctx.Process(target=_rank, args=(r, 2, port, name, q)) for r in range(2)]
     for pr in procs:
         pr.start()
-    for pr in procs:
-        pr.join(120)
-        assert pr.exitcode == 0
+    _join_all(procs, 120)
     assert q.get(timeout=5) <= 1e-14
 
 
@@ -225,8 +236,6 @@ def test_two_gloo_ranks_partitioned_pcg(name):
     procs = [ctx.Process(target=_pcg_rank, args=(r, 2, port, name, q)) for r in range(2)]
     for pr in procs:
         pr.start()
-    for pr in procs:
-        pr.join(300)
-        assert pr.exitcode == 0
+    _join_all(procs, 300)
     err, it, it_o = q.get(timeout=5)
     assert err <= 1e-10 and abs(it - it_o) <= 2, (err, it, it_o)

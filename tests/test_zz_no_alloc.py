@@ -14,6 +14,7 @@ import numpy as np
 import pytest
 
 import elastic_gb300 as E
+import oracle as O
 from elastic_gb300 import meshgen as M
 from helpers import rel_inf
 
@@ -67,6 +68,9 @@ def test_noalloc_matches_context_spmv(built_lib):
             torch.cuda.synchronize(dev)
             y = d_y.cpu().numpy()
             assert rel_inf(y_ref, y) <= SPMV_TOL, f"call {call}"
+            # and the oracle's matvec_csrcsym1 (Matvec.f:528-621) on the same arrays
+            s = O.Structure(perm=st.perm, id=st.id, neq=neq, nad=nad, ia=st.ia, ja=st.ja)
+            assert rel_inf(O.matvec(s, ad, al, x), y) <= SPMV_TOL, f"call {call}"
             xy_ref = float(x @ y_ref)
             assert abs(d_xy.item() - xy_ref) <= DOT_TOL * abs(xy_ref), f"call {call}"
         # sizes beyond the scratch's maximum are refused before any GPU work
