@@ -253,6 +253,9 @@ def run_ours(args, dist: Dist):
             mixed_pcg_ms.append(e2.elapsed_time(e1))
     xm = ctx.solution()
     spmv32_ms = time_spmv(E.PREC_MIXED)
+    # device bytes the context holds with both solvers' data resident: mesh,
+    # structure, CSRC ad / al, the sliced FP64 and FP32 copies, vectors
+    device_bytes = ctx.device_bytes
     spmv32_bytes = 8 * nad + 16 * neq
     clk = clocks.stop()
     mixed_step = dist.max(statistics.median(mixed_ms))
@@ -324,18 +327,27 @@ def run_ours(args, dist: Dist):
            "partitioned_spmv": part}
 
     # the FP64 product's floor on this part: one DFMA per stored entry of the
-    # full matrix (2 nad + neq) at 2 DFMA per clock per SM (measured with a
-    # register-only FMA loop), at the SM clock sampled during the run
+    # full matrix (2 nad + neq) at the FP64 pipe's rate, measured here by the
+    # library's register-only probe (elx_fp64_fma_rate), scaled to the SM
+    # clock sampled during the run
     sms = torch.cuda.get_device_properties(dev).multi_processor_count
     mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz")
+    fma_rate, per_clk = E.fp64_fma_rate(dev)
     fp64_floor = None
     if mhz:
         dfma = 2 * nad + neq
-        floor_us = dfma / (2.0 * sms * mhz * 1e6) * 1e6
-        fp64_floor = {"dfma_per_launch": dfma, "dfma_per_clock_per_sm": 2, "sms": sms,
-                      "sm_mhz": mhz, "floor_us": floor_us,
-                      "floor_gbs": spmv_bytes / (floor_us * 1e-6) / 1e9,
-                      "frac_of_floor": floor_us / (spmv_ms * 1e3)}
+        floor_us = dfma / (per_clk * sms * mhz * 1e6) * 1e6
+        # the pipe's nominal rate (2 per clock per SM: what ncu counts as
+        # 100 % busy) gives the hard floor; the probe reaches 84 % of it
+        nominal_us = dfma / (2.0 * sms * mhz * 1e6) * 1e6
+        fp64_floor = {"dfma_per_launch": dfma, "dfma_per_clock_per_sm_probe": per_clk,
+                      "probe_fma_per_s": fma_rate, "sms": sms,
+                      "sm_mhz": mhz, "floor_us_probe": floor_us,
+                      "floor_frac_of_hbm_probe": spmv_bytes / (floor_us * 1e-6) / 1e9 / peak,
+                      "frac_of_floor_probe": floor_us / (spmv_ms * 1e3),
+                      "floor_us_nominal": nominal_us,
+                      "floor_frac_of_hbm_nominal": spmv_bytes / (nominal_us * 1e-6) / 1e9 / peak,
+                      "frac_of_floor_nominal": nominal_us / (spmv_ms * 1e3)}
 
     out = None
     if dist.rank == 0:
@@ -346,9 +358,7 @@ def run_ours(args, dist: Dist):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (structured mesh generated in-process)",
-            "config": {"workload": WORKLOAD, "neq": neq, "nad": nad, "colors": ncolors,
-                       "tol": TOL, "parallelism": "replicas" if n > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (CSRC matrix 400 MB + vectors > 129 MB L2)"},
+            "config": bench_config(neq, nad, n), "colors": ncolors,
             "time_to_tol_ms": ms_step, "pcg_iters": iters, "assembly_ms": asm_ms,
             "pcg_ms": pcg_ms, "pcg_iter_gbs": iter_gbs, "spmv_ms": spmv_ms,
             "spmv_gbs": spmv_gbs, "wall_s": wall,
@@ -373,13 +383,28 @@ def run_ours(args, dist: Dist):
             "e2e": {"value": n / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
+            "device_bytes": device_bytes,
+            "csrc_bytes": 8 * (nad + neq) + 4 * (nad + neq + 1),
             "clocks": clk,
         }
         if n == 1 and not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(mesh, st, b0, u0, iters, sample_iters=300)
+            import oracle as O
+            s_o = O.structure(mesh, True)
+            b0_o, u0_o = O.loads(mesh, s_o)
+            out["cpu_baseline"] = cpu_baseline(mesh, s_o, b0_o, u0_o, keep=True)
+            # the FP64 and mixed solutions against the oracle's pcg_omp solve
+            # (the same equations: the structures are the same bit for bit)
+            x_o = out["cpu_baseline"].pop("_x")
+            same = all(np.array_equal(a, b) for a, b in
+                       ((s_o.perm, st.perm), (s_o.id, st.id), (s_o.ia, st.ia), (s_o.ja, st.ja)))
+            rel = lambda a: float(np.abs(a - x_o).max() / np.abs(x_o).max())
+            out["parity_vs_oracle"] = {
+                "structure_bit_exact": same, "oracle_pcg_iters": out["cpu_baseline"]["pcg_iters"],
+                "gpu_pcg_iters": iters, "rel_err_fp64": rel(x64), "rel_err_mixed": rel(xm),
+                "bars": ("FP64 <= 1e-9 with iterations +-2 at tol 1e-8 (the oracle's own "
+                         "pcg_omp moves by 4.4e-10 between 8 and 5 threads here); mixed <= 1e-7")}
             # the oracle's stress recovery (one host thread) on the same u,
             # and how far the device's nodal stresses are from it
-            import oracle as O
             t = time.perf_counter()
             t_o = O.tform(mesh, u_sol)
             nxt["stress_cpu_oracle_ms"] = 1e3 * (time.perf_counter() - t)
@@ -472,14 +497,25 @@ def run_block(args):
             times.append(e0.elapsed_time(e1))
     X = dX.cpu().numpy().T
     ms = statistics.median(times)
-    # single-RHS FP64 PCG on two of the cases, timed the same way
-    single = []
+    # single-RHS FP64 PCG on two of the cases, timed the same way, and the
+    # oracle's FP64 pcg_omp of the same two cases on this host's cores
+    import oracle as O
+    nth = len(os.sched_getaffinity(0))
+    s = O.Structure(perm=st.perm, id=st.id, neq=st.neq, nad=st.nad, ia=st.ia, ja=st.ja)
+    ad_o, al_o, _ = O.assemble_omp(mesh, s, np.zeros((mesh.nnode, mesh.ndf)), np.zeros(neq),
+                                   nthreads=nth)
+    single, err_block, err_single, o_iters, o_s = [], {}, {}, {}, []
     for c in range(2):
         ctx.solve(B[:, c], tol=TOL, maxit=MAXIT)  # warm
         t = time.perf_counter()
         x, info = ctx.solve(B[:, c], tol=TOL, maxit=MAXIT)
         single.append((time.perf_counter() - t) * 1000.0)
-        err = float(np.abs(x - X[:, c]).max() / np.abs(x).max())
+        x_o, i_o = O.pcg_omp(s, ad_o, al_o, B[:, c], tol=TOL, maxit=MAXIT, nthreads=nth)
+        o_s.append(i_o["seconds"])
+        o_iters[str(c)] = [i_o["iters"], info["iters"]]
+        rel = lambda a: float(np.abs(a - x_o).max() / np.abs(x_o).max())
+        err_block[str(c)] = rel(X[:, c])
+        err_single[str(c)] = rel(x)
     its = [i["iters"] for i in infos]
     ctx.close()
     single_ms = statistics.mean(single)
@@ -490,7 +526,54 @@ def run_block(args):
             "replacements": infos[0]["refinements"],
             "single_fp64_ms_per_case": single_ms,
             "speedup_per_case_vs_single_fp64": single_ms / (ms / 16),
-            "rel_err_vs_fp64_case0": err}
+            "rel_err_block_mixed_vs_oracle_by_case": err_block,
+            "rel_err_single_fp64_vs_oracle_by_case": err_single,
+            "oracle_vs_single_fp64_iters_by_case": o_iters,
+            "oracle_pcg_omp_s_per_case": statistics.mean(o_s), "oracle_cores": nth}
+
+
+def run_fp64peak(args):
+    """The FP64 pipe's FMA rate (the library's register-only probe kernel),
+    the denominator of the FP64 product's floor."""
+    import torch
+
+    import elastic_gb300 as E
+
+    p = torch.cuda.get_device_properties(0)
+    E.fp64_fma_rate(0)  # warm
+    clocks = ClockSampler(0)
+    clocks.start()
+    runs = [E.fp64_fma_rate(0) for _ in range(max(args.steps, 8))]
+    clk = clocks.stop()
+    rate = max(r for r, _ in runs)
+    out = {"mode": "fp64peak", "fma_per_s": rate, "tflops": 2 * rate / 1e12,
+           "fma_per_clock_per_sm_at_max_clock": max(c for _, c in runs),
+           "sms": p.multi_processor_count, "clocks": clk}
+    if clk and clk.get("sm_mhz"):
+        out["fma_per_clock_per_sm_at_sampled_clock"] = (
+            rate / (p.multi_processor_count * clk["sm_mhz"] * 1e6))
+    return out
+
+
+def run_spmm(args):
+    """The block products of the 96x96x48 plate alone: the autotuner's times
+    of every width (FP32 and FP64, with the fused dots), for profiling."""
+    import elastic_gb300 as E
+    from elastic_gb300 import meshgen as M
+
+    mesh, _ = M.plate_hexa8_96(16)
+    ctx = E.Context(device=0)
+    ctx.set_mesh(mesh)
+    neq, nad, _ = ctx.build_structure(True)
+    ctx.assemble(None, None)
+    out = {"mode": "spmm", "neq": neq, "nad": nad}
+    for _ in range(max(1, args.steps)):
+        for name, prec in (("fp32", E.PREC_MIXED), ("fp64", E.PREC_FP64)):
+            w, tt = ctx.autotune_block(prec, remeasure=True)
+            out[name] = {"width": w, "us_by_width": dict(zip(["1", "2", "4", "8", "16"],
+                                                             np.round(tt, 1).tolist()))}
+    ctx.close()
+    return out
 
 
 def run_tetra(args):
@@ -613,7 +696,7 @@ def run_serve(args):
 
     th = threading.Thread(target=submitter)
     th.start()
-    lat, done_at, errs, bad = [], [], [], 0
+    lat, done_at, errs, bad, served_u = [], [], [], 0, {}
     for i in range(n):
         while tickets[i] is None:
             time.sleep(0.001)
@@ -624,15 +707,41 @@ def run_serve(args):
         done_at.append(t_sub - t_start + latency)
         if i in ref_u:
             errs.append(float(np.abs(U - ref_u[i]).max() / max(np.abs(ref_u[i]).max(), 1e-300)))
+            served_u[i] = U
     th.join()
     stats = srv.stats()
-    # the same requests all at once (a closed batch): the server's capacity
-    t0 = time.perf_counter()
-    tks = [srv.submit(m, F, tol=TOL, maxit=MAXIT) for m, F in reqs]
-    for tk in tks:
-        srv.wait(tk, timeout=3600)
-    sat_span = time.perf_counter() - t0
+    sat_span = None
+    if args.all_at_once:
+        # the same requests all at once (a closed batch): the server's capacity
+        t0 = time.perf_counter()
+        tks = [srv.submit(m, F, tol=TOL, maxit=MAXIT) for m, F in reqs]
+        for tk in tks:
+            srv.wait(tk, timeout=3600)
+        sat_span = time.perf_counter() - t0
     srv.close()
+    # sampled served results against the oracle's FP64 solves (pcg_omp on this
+    # host's cores, the oracle's own structure and assembly): requests of up
+    # to 3e5 dofs among the sampled ones; the packed loop solves them in FP64
+    # (<= 1e5 dofs), the block solver in mixed precision for 3-D meshes above
+    import oracle as O
+    nth = len(os.sched_getaffinity(0))
+    err_o = {"fp64_packed": [], "block": []}
+    for i in sorted(served_u):
+        m, F = reqs[i]
+        if m.nnode * m.ndf > 3e5:
+            continue
+        s = O.structure(m, True)
+        ad, al, _ = O.assemble_omp(m, s, np.zeros((m.nnode, m.ndf)), np.zeros(s.neq),
+                                   nthreads=nth)
+        free = s.id > 0
+        for k in range(F.shape[0]):
+            b = np.zeros(s.neq)
+            b[s.id[free] - 1] = F[k][free]
+            x, _ = O.pcg_omp(s, ad, al, b, tol=TOL, maxit=MAXIT, nthreads=nth)
+            u = np.zeros_like(F[k])
+            u[free] = x[s.id[free] - 1]
+            d = float(np.abs(served_u[i][k] - u).max() / max(np.abs(u).max(), 1e-300))
+            err_o["block" if s.neq >= 1e5 else "fp64_packed"].append(d)
     span = max(done_at)
     pct = lambda v, q: float(np.percentile(np.array(v), q))
     return {"mode": "serve", "requests": n, "load_cases": cases,
@@ -643,78 +752,95 @@ def run_serve(args):
                        "peak_device_bytes": stats["peak_bytes"],
                        "peak_load_cases_in_pack": stats["peak_slots"],
                        "packed_iterations": stats["iterations"],
-                       "all_at_once_solves_per_s": cases / sat_span},
+                       "all_at_once_solves_per_s": cases / sat_span if sat_span else None},
             "sequential_fp64": {"solves_per_s": cases / seq_span, "requests_per_s": n / seq_span,
                                 "p50_latency_s": pct(lat_seq, 50),
                                 "p99_latency_s": pct(lat_seq, 99), "span_s": seq_span,
                                 "mean_service_s": statistics.mean(service)},
-            "max_rel_diff_vs_sequential_sample": max(errs) if errs else None}
+            "max_rel_diff_vs_sequential_sample": max(errs) if errs else None,
+            "vs_oracle_fp64": {
+                "requests": sum(1 for i in served_u if reqs[i][0].nnode * reqs[i][0].ndf <= 3e5),
+                "load_cases": {k: len(v) for k, v in err_o.items()},
+                "max_rel_err": {k: (max(v) if v else None) for k, v in err_o.items()},
+                "bars": "packed FP64 <= 1e-9; block (mixed for 3-D) <= 1e-6"}}
 
 
 # ------------------------------------------------------------------ CPU side
-def cpu_baseline(mesh, st, b0, u0, full_iters=None, sample_iters=300, nthreads=None):
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), with the logical CPUs this process
+    may use."""
+    name = ""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return f"{name or 'unknown'} ({len(os.sched_getaffinity(0))} logical CPUs usable)"
+
+
+def bench_config(neq, nad, n_ranks):
+    """The workload description both arms print (the same keys and values)."""
+    return {"workload": WORKLOAD, "neq": neq, "nad": nad, "tol": TOL,
+            "parallelism": "replicas" if n_ranks > 1 else "single",
+            "l2": "inputs larger than L2 (CSRC matrix 400 MB + vectors > 129 MB L2)"}
+
+
+def cpu_baseline(mesh, s, b0, u0, nthreads=None, sequential=True, keep=False):
     """The reference's OpenMP CPU path (oracle restatement of pform_mec's
     colour loop and pcg_omp with matvec_csrcsym_omp) on this host's cores:
-    one full assembly plus a bounded PCG sample, extrapolated to the
-    iteration count of the full solve."""
+    one full assembly and one full PCG solve, timed; with `sequential`, also
+    the one-thread path (pform_mec's element loop, matvec_csrcsym1, pcg);
+    with `keep`, the OpenMP solve's x under "_x"."""
     import oracle as O
 
     nth = nthreads or len(os.sched_getaffinity(0))
-    s = O.Structure(perm=st.perm, id=st.id, neq=st.neq, nad=st.nad, ia=st.ia, ja=st.ja)
     colors = O.colormsh(mesh)
     t = time.perf_counter()
     ad, al, b = O.assemble_omp(mesh, s, u0, b0, nthreads=nth, colors=colors)
     t_asm = time.perf_counter() - t
-    if full_iters is None:
-        _, info = O.pcg_omp(s, ad, al, b, tol=TOL, maxit=MAXIT, nthreads=nth)
-        full_iters = info["iters"]
-        t_pcg = info["seconds"]
-        sample = f"full assembly + full PCG ({full_iters} iterations)"
-    else:
-        n = min(sample_iters, full_iters)
-        _, info = O.pcg_omp(s, ad, al, b, tol=TOL, maxit=n, nthreads=nth, stop_at_maxit=True)
-        t_pcg = info["seconds"] * full_iters / max(info["iters"], 1)
-        sample = (f"full OpenMP assembly + {info['iters']} PCG iterations, scaled to "
-                  f"{full_iters} iterations")
+    x_o, info = O.pcg_omp(s, ad, al, b, tol=TOL, maxit=MAXIT, nthreads=nth)
+    t_pcg = info["seconds"]
     total = t_asm + t_pcg
-    # the sequential path (pform_mec's element loop, matvec_csrcsym1 and pcg
-    # on one thread): one full assembly and a 30-iteration sample
-    t = time.perf_counter()
-    O.assemble(mesh, s, u0, b0)
-    t_asm1 = time.perf_counter() - t
-    n1 = min(30, full_iters)
-    _, info1 = O.pcg(s, ad, al, b, tol=TOL, maxit=n1)
-    t_pcg1 = info1["seconds"] * full_iters / max(info1["iters"], 1)
-    return {"value": 1.0 / total, "unit": "solves/s", "cores": nth, "kind": "port",
-            "sample": sample, "seconds_per_solve": total, "assembly_s": t_asm,
-            "pcg_s": t_pcg,
-            "sequential_1thread": {"value": 1.0 / (t_asm1 + t_pcg1), "unit": "solves/s",
-                                   "cores": 1, "assembly_s": t_asm1, "pcg_s": t_pcg1,
-                                   "sample": f"full assembly + {info1['iters']} PCG "
-                                             f"iterations, scaled to {full_iters}"}}
+    out = {"value": 1.0 / total, "unit": "solves/s", "cores": nth, "kind": "port",
+           "cpu": cpu_model(),
+           "sample": f"one full OpenMP assembly + one full pcg_omp solve ({info['iters']} "
+                     "iterations), no extrapolation",
+           "seconds_per_solve": total, "assembly_s": t_asm, "pcg_s": t_pcg,
+           "pcg_iters": info["iters"]}
+    if sequential:
+        t = time.perf_counter()
+        O.assemble(mesh, s, u0, b0)
+        t_asm1 = time.perf_counter() - t
+        _, info1 = O.pcg(s, ad, al, b, tol=TOL, maxit=MAXIT)
+        out["sequential_1thread"] = {
+            "value": 1.0 / (t_asm1 + info1["seconds"]), "unit": "solves/s", "cores": 1,
+            "assembly_s": t_asm1, "pcg_s": info1["seconds"], "pcg_iters": info1["iters"],
+            "sample": "one full assembly + one full pcg solve on one thread"}
+    if keep:
+        out["_x"] = x_o  # the solution (the caller's parity check; not printed)
+    return out
 
 
 def run_reference(args, dist: Dist):
     """--impl reference: the reference's CPU implementation of the path (the
-    oracle port: OpenMP assembly + pcg_omp) on this host's cores."""
+    oracle port, with its own structure: graph, RCM, numeq, csrstruct; then
+    per step the OpenMP assembly and the full pcg_omp solve) on this host's
+    cores.  Under torchrun only rank 0 runs."""
     if dist.rank != 0:
         return None
-    import elastic_gb300 as E
     import oracle as O
 
     mesh = make_workload()
-    st = E.host_structure(mesh, True)
-    b0, u0 = E.pload(mesh, st.id)
-    s = O.Structure(perm=st.perm, id=st.id, neq=st.neq, nad=st.nad, ia=st.ia, ja=st.ja)
+    s = O.structure(mesh, True)
+    b0, u0 = O.loads(mesh, s)
     nth = len(os.sched_getaffinity(0))
-    colors = O.colormsh(mesh)
-    # the full solve's iteration count, once (needed to scale the samples)
-    ad, al, b = O.assemble_omp(mesh, s, u0, b0, nthreads=nth, colors=colors)
-    _, info = O.pcg_omp(s, ad, al, b, tol=TOL, maxit=MAXIT, nthreads=nth)
-    full_iters = info["iters"]
-    per_step = []
+    per_step, iters = [], None
     for k in range(args.warmup + args.steps):
-        r = cpu_baseline(mesh, st, b0, u0, full_iters, sample_iters=150, nthreads=nth)
+        r = cpu_baseline(mesh, s, b0, u0, nthreads=nth, sequential=False)
+        iters = r["pcg_iters"]
         if k >= args.warmup:
             per_step.append(r["seconds_per_solve"])
     sec = statistics.median(per_step)
@@ -723,13 +849,14 @@ def run_reference(args, dist: Dist):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
         "n_gpus": dist.ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec * 1000.0, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (structured mesh)",
-        "config": {"workload": WORKLOAD, "neq": st.neq, "nad": st.nad, "tol": TOL,
-                   "parallelism": f"OpenMP {nth} threads"},
-        "pcg_iters": full_iters,
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (structured mesh generated in-process)",
+        "config": bench_config(s.neq, s.nad, dist.ws),
+        "pcg_iters": iters,
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nth, "kind": "port",
-                         "sample": ("per step: full OpenMP assembly + 150 pcg_omp iterations "
-                                    f"scaled to the full solve's {full_iters} iterations")},
+                         "cpu": cpu_model(),
+                         "sample": ("per step: one full OpenMP assembly + one full pcg_omp "
+                                    f"solve ({iters} iterations); median of {args.steps} steps "
+                                    f"after {args.warmup}")},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -744,9 +871,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="full mode: skip the block, tetra and serve sub-benchmarks")
-    ap.add_argument("--mode", choices=["full", "spmv", "block", "tetra", "serve"],
+    ap.add_argument("--mode", choices=["full", "spmv", "spmm", "block", "tetra", "serve",
+                                       "fp64peak"],
                     default="full",
-                    help="spmv: only the SpMV of the workload (for profiling); block: 16 load "
+                    help="spmv: only the SpMV of the workload (for profiling); spmm: only the "
+                         "block products of the 96x96x48 plate (profiling); block: 16 load "
                          "cases on the 96x96x48 plate; tetra: FP64 and mixed PCG on the "
                          "48^3 TETRA4 mesh; serve: the served request stream")
     ap.add_argument("--requests", type=int, default=512, help="serve: requests in the stream")
@@ -763,22 +892,27 @@ def main():
             out = run_spmv_only(args)
         elif args.mode == "block":
             out = run_block(args)
+        elif args.mode == "spmm":
+            out = run_spmm(args)
+        elif args.mode == "fp64peak":
+            out = run_fp64peak(args)
         elif args.mode == "tetra":
             out = run_tetra(args)
         elif args.mode == "serve":
+            args.all_at_once = True
             out = run_serve(args)
         else:
             out = run_ours(args, dist)
             if out is not None and dist.ws == 1 and not args.no_extras:
-                # the other headline workloads, at their own sizes (block, tetra)
-                # and on a shortened stream (serve: 64 requests up to 2e5 dofs;
-                # the full 512-request stream is --mode serve)
+                # the other headline workloads at their own sizes: block, tetra
+                # and the served stream (512 requests, 2k-2M dofs; --mode serve
+                # also measures the same requests submitted all at once)
                 blk = argparse.Namespace(**vars(args))
                 blk.steps, blk.warmup = 3, 3
                 out["block"] = run_block(blk)
                 out["tetra"] = run_tetra(blk)
                 srv = argparse.Namespace(**vars(args))
-                srv.requests, srv.max_dof = 64, 2e5
+                srv.all_at_once = False
                 out["serve"] = run_serve(srv)
     finally:
         dist.close()
