@@ -519,7 +519,20 @@ def run_block(args):
     its = [i["iters"] for i in infos]
     ctx.close()
     single_ms = statistics.mean(single)
+    # the block product's roofline: FP32 algorithmic bytes of one product of
+    # the autotuned width (8 nad + 8 neq + 8 W neq) over its timed launch
+    peak, peak_kind = measured_peak()
+    w_us = dict(zip([1, 2, 4, 8, 16], tt))[width]
+    spmm_bytes = 8 * nad + 8 * neq + 8 * width * neq
+    spmm_gbs = spmm_bytes / (w_us * 1e-6) / 1e9
     return {"mode": "block", "workload": "HEXA8 plate 96x96x48, 16 load cases, tol 1e-8",
+            "spmm_roofline": {"kernel": f"sell_spmm_kernel<float, 3, {width}>",
+                              "bound": "hbm", "achieved": spmm_gbs, "peak": peak,
+                              "unit": "GB/s", "frac": spmm_gbs / peak, "peak_kind": peak_kind,
+                              "algorithmic_bytes_per_launch": spmm_bytes, "us": w_us,
+                              "traffic": profiled("traffic_bytes_per_launch",
+                                                  "sell_spmm_fp32_w16_hexa8_plate96.md")
+                              if width == 16 else None},
             "neq": neq, "nad": nad, "block_width": width,
             "spmm32_us_by_width": dict(zip(["1", "2", "4", "8", "16"], np.round(tt, 1).tolist())),
             "ms_16_cases": ms, "ms_per_case": ms / 16, "iters_min_max": [min(its), max(its)],
