@@ -77,13 +77,18 @@ def test_cube64_hexa8_against_oracle(built_lib):
 def test_tetra4_48_mixed_materials_against_oracle(built_lib):
     """The 48^3 TETRA4 mesh with jittered nodes and one lognormal E per
     element (345,744 equations), tol 1e-10: FP64 PCG within 1e-10 of the
-    oracle's pcg_omp, the mixed solver within 1e-9 (8.4e-11 measured)."""
+    oracle's pcg_omp, the mixed solver within 1e-9 (8.4e-11 measured).  At
+    ~2,450 iterations the count itself moves with the summation order: the
+    oracle takes 2446-2449 iterations on 2-8 OpenMP threads and 2452
+    sequentially (solutions within 4e-12 of each other), so the bar is 0.5 %
+    (12 iterations) here rather than 2."""
     m = M.cube_tetra4_48_mixed()
     with E.Context(device=0) as ctx:
         s, ad, al, b = _assembled(ctx, m)
         x_o, i_o = O.pcg_omp(s, ad, al, b, tol=1e-10, maxit=20000, nthreads=NTH)
         x_g, i_g = ctx.solve(b, tol=1e-10, maxit=20000)
-        assert abs(i_o["iters"] - i_g["iters"]) <= 2, (i_o["iters"], i_g["iters"])
+        assert abs(i_o["iters"] - i_g["iters"]) <= 0.005 * i_o["iters"], \
+            (i_o["iters"], i_g["iters"])
         assert rel_inf(x_o, x_g) <= 1e-10
         x_m, i_m = ctx.solve(b, tol=1e-10, maxit=20000, precision=E.PREC_MIXED)
         assert i_m["norm_m_r"] <= i_m["conv"] * (1 + 1e-6)
