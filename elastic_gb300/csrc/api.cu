@@ -1009,12 +1009,16 @@ const char *elx_version(void) { return "elastic_gb300 0.1 (sm_103a)"; }
 
 int elx_fp64_fma_rate(int32_t device, double *fma_per_s, double *per_clock_per_sm) {
   if (!fma_per_s) return ELX_ERR_ARG;
+  int prev = 0;
+  if (cudaGetDevice(&prev) != cudaSuccess) return ELX_ERR_CUDA;
+  int code = ELX_OK;
   try {
     *fma_per_s = elx::measure_fp64_fma_rate(device, per_clock_per_sm);
-    return ELX_OK;
   } catch (const Error &e) {
-    return e.code;
+    code = e.code;
   }
+  cudaSetDevice(prev);  // the caller's current device, as it was
+  return code;
 }
 
 int elx_create(elx_ctx **out, const elx_opts *opts) {

@@ -355,7 +355,9 @@ int elx_partition_info(elx_ctx *ctx, int32_t nparts, int32_t part, int32_t *eq0,
  * resident wave, best of five timed launches) and, if per_clock_per_sm is
  * not NULL, that rate per clock per SM at the device's maximum SM clock.
  * No reference counterpart: the FP64 product's floor (one FMA per stored
- * entry of the full matrix) is this rate. */
+ * entry of the full matrix) is this rate.  The call allocates and frees one
+ * output buffer (a double per probe thread) and leaves the calling thread's
+ * current device as it found it. */
 int elx_fp64_fma_rate(int32_t device, double *fma_per_s, double *per_clock_per_sm);
 
 /* Test hook of the device number formatter: n fields Ew.d (e = 0) or
