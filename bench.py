@@ -922,13 +922,19 @@ def main():
                 # the other headline workloads at their own sizes: block, tetra
                 # and the served stream (512 requests, 2k-2M dofs; --mode serve
                 # also measures the same requests submitted all at once)
+                # (a failure in one of them is recorded in its sub-object and
+                # the line is still printed)
                 blk = argparse.Namespace(**vars(args))
                 blk.steps, blk.warmup = 3, 3
-                out["block"] = run_block(blk)
-                out["tetra"] = run_tetra(blk)
                 srv = argparse.Namespace(**vars(args))
                 srv.all_at_once = False
-                out["serve"] = run_serve(srv)
+                for key, fn, a in (("block", run_block, blk), ("tetra", run_tetra, blk),
+                                   ("serve", run_serve, srv)):
+                    try:
+                        out[key] = fn(a)
+                    except Exception as e:  # noqa: BLE001 -- reported, not hidden
+                        out[key] = {"error": f"{type(e).__name__}: {e}"}
+                        print(f"bench: {key} failed: {e}", file=sys.stderr)
     finally:
         dist.close()
     if out is not None and dist.rank == 0:
