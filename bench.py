@@ -481,6 +481,7 @@ def run_block(args):
         B[st.id[free] - 1, c] = F[c][free]
     ctx.assemble(None, None)
     width, tt = ctx.autotune_block(E.PREC_MIXED, remeasure=True)
+    tiling = ctx.block_tiling(E.PREC_MIXED)
     dB = torch.from_numpy(np.ascontiguousarray(B.T)).cuda()
     dX = torch.zeros_like(dB)
     ext = torch.cuda.ExternalStream(ctx.stream, device=0)
@@ -535,6 +536,7 @@ def run_block(args):
                               if width == 16 else None},
             "neq": neq, "nad": nad, "block_width": width,
             "spmm32_us_by_width": dict(zip(["1", "2", "4", "8", "16"], np.round(tt, 1).tolist())),
+            "spmm32_groups_in_flight_by_width": dict(zip(["1", "2", "4", "8", "16"], tiling)),
             "ms_16_cases": ms, "ms_per_case": ms / 16, "iters_min_max": [min(its), max(its)],
             "replacements": infos[0]["refinements"],
             "single_fp64_ms_per_case": single_ms,
@@ -584,7 +586,9 @@ def run_spmm(args):
         for name, prec in (("fp32", E.PREC_MIXED), ("fp64", E.PREC_FP64)):
             w, tt = ctx.autotune_block(prec, remeasure=True)
             out[name] = {"width": w, "us_by_width": dict(zip(["1", "2", "4", "8", "16"],
-                                                             np.round(tt, 1).tolist()))}
+                                                             np.round(tt, 1).tolist())),
+                         "groups_in_flight_by_width": dict(zip(["1", "2", "4", "8", "16"],
+                                                               ctx.block_tiling(prec)))}
     ctx.close()
     return out
 

@@ -139,6 +139,7 @@ def load():
         "elx_solve_block_device": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_double, C.c_int32,
                                              C.c_int32, _VP, _VP, _VP]),
         "elx_autotune_block": (C.c_int, [_VP, C.c_int32, P(C.c_int32), _VP]),
+        "elx_block_tiling": (C.c_int, [_VP, C.c_int32, _VP]),
         "elx_stress": (C.c_int, [_VP, _VP, _VP, _VP]),
         "elx_update_resident": (C.c_int, [_VP]),
         "elx_set_loads": (C.c_int, [_VP, _VP, _VP, _VP, C.c_int32]),
@@ -465,6 +466,13 @@ class Context:
         self._check(self._L.elx_autotune_block(self._h, precision, C.byref(w),
                                                t.ctypes.data_as(_VP) if remeasure else None))
         return w.value, (t if remeasure else None)
+
+    def block_tiling(self, precision=PREC_MIXED):
+        """The autotuner's slot groups in flight of the block product for
+        widths 1, 2, 4, 8, 16 (0: not tuned)."""
+        u = np.zeros(5, np.int32)
+        self._check(self._L.elx_block_tiling(self._h, precision, u.ctypes.data_as(_VP)))
+        return u.tolist()
 
     def spmv(self, x, precision=PREC_FP64):
         neq, _, _ = self.sizes()

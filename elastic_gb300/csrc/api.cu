@@ -193,6 +193,8 @@ void upload_structure(elx_ctx *c, bool prederived) {
     c->release(*v);
   release_block(c);
   c->tuned_width[0] = c->tuned_width[1] = 0;
+  for (auto &row : c->tuned_unroll)
+    for (int &u : row) u = 0;
   for (DBuf *v : {&c->node_count, &c->tstress, &c->tx0buf, &c->fbuf, &c->ld_node, &c->ld_ptr,
                   &c->ld_ent, &c->ld_vec, &c->vtkbuf})
     c->release(*v);
@@ -723,9 +725,12 @@ elx::BlockVecs block_vecs(elx_ctx *c, int w) {
   return v;
 }
 
-// The block width whose product costs least per column: each supported
-// width's SpMM timed on the resident matrix (FP32 for the mixed solver, FP64
-// otherwise), best of three launches after one warm-up.
+// The block width whose product costs least per column, and per width the
+// product's tiling: each supported width's product timed on the resident
+// matrix (FP32 for the mixed solver, FP64 otherwise; the solver's own form,
+// with the fused dots), best of three launches after one warm-up, for 1, 2
+// and 3 slot groups of matrix loads in flight (3x3 node blocks; 2x2 blocks
+// have one form), the fastest kept.  ELX_SPMM_UNROLL fixes the tiling.
 int autotune_block_width(elx_ctx *c, bool mixed, double *times_us = nullptr) {
   const int slot = mixed ? 1 : 0;
   if (c->tuned_width[slot] && !times_us) return c->tuned_width[slot];
@@ -734,35 +739,48 @@ int autotune_block_width(elx_ctx *c, bool mixed, double *times_us = nullptr) {
   const size_t n = (size_t)c->s.neq;
   ELX_CUDA(cudaMemsetAsync(c->bk_p.p, 0, n * kMaxBlockWidth * 8, c->stream));
   if (mixed) ELX_CUDA(cudaMemsetAsync(c->bk_p32.p, 0, n * kMaxBlockWidth * 4, c->stream));
-  const elx::CsrcDev k = c->csrc_dev();
+  const bool tile = c->s.bsize == 3 && c->spmm_unroll == 0;
   int best = 1;
   double best_cost = 1e300;
   int idx = 0;
   for (int w : {1, 2, 4, 8, 16}) {
     const elx::BlockVecs v = block_vecs(c, w);
-    double t_best = 1e300;
-    for (int rep = 0; rep < 4; rep++) {
-      ELX_CUDA(cudaEventRecord(c->ev_t[0], c->stream));
-      if (mixed)
-        elx::launch_spmm32(k, v, c->stream);
-      else
-        elx::launch_spmm64(k, v, c->stream);
-      ELX_CUDA(cudaEventRecord(c->ev_t[1], c->stream));
-      ELX_CUDA(cudaEventSynchronize(c->ev_t[1]));
-      float ms = 0.f;
-      ELX_CUDA(cudaEventElapsedTime(&ms, c->ev_t[0], c->ev_t[1]));
-      if (rep > 0) t_best = std::min(t_best, (double)ms);
+    double t_w = 1e300;
+    int u_w = 0;
+    for (int u : {1, 2, 3}) {
+      if (!tile && u > 1) break;
+      c->tuned_unroll[slot][idx] = tile ? u : 0;
+      const elx::CsrcDev k = c->csrc_dev();
+      double t_best = 1e300;
+      for (int rep = 0; rep < 4; rep++) {
+        ELX_CUDA(cudaEventRecord(c->ev_t[0], c->stream));
+        if (mixed)
+          elx::launch_spmm32(k, v, c->stream);
+        else
+          elx::launch_spmm64(k, v, c->stream);
+        ELX_CUDA(cudaEventRecord(c->ev_t[1], c->stream));
+        ELX_CUDA(cudaEventSynchronize(c->ev_t[1]));
+        float ms = 0.f;
+        ELX_CUDA(cudaEventElapsedTime(&ms, c->ev_t[0], c->ev_t[1]));
+        if (rep > 0) t_best = std::min(t_best, (double)ms);
+      }
+      c->launches += 4;
+      if (t_best < t_w) {
+        t_w = t_best;
+        u_w = tile ? u : 0;
+      }
     }
-    c->launches += 4;
-    if (times_us) times_us[idx] = t_best * 1e3;
+    c->tuned_unroll[slot][idx] = u_w;
+    if (times_us) times_us[idx] = t_w * 1e3;
     idx++;
-    const double cost = t_best / w;
+    const double cost = t_w / w;
     if (cost < best_cost * 0.97) {  // a wider block must win by 3 %
       best_cost = cost;
       best = w;
     }
   }
   c->tuned_width[slot] = best;
+  c->drop_graphs();  // a captured block iteration holds the earlier tiling
   return best;
 }
 
@@ -1619,6 +1637,14 @@ int elx_autotune_block(elx_ctx *c, int32_t precision, int32_t *width, double *ti
     const bool mixed = precision == ELX_PREC_MIXED;
     if (times_us) c->tuned_width[mixed ? 1 : 0] = 0;
     *width = autotune_block_width(c, mixed, times_us);
+  });
+}
+
+int elx_block_tiling(elx_ctx *c, int32_t precision, int32_t *unroll) {
+  return guarded(c, [&] {
+    require(unroll, ELX_ERR_ARG, "null unroll");
+    const int slot = precision == ELX_PREC_MIXED ? 1 : 0;
+    for (int i = 0; i < 5; i++) unroll[i] = c->tuned_unroll[slot][i];
   });
 }
 

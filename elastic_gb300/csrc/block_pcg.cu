@@ -720,9 +720,12 @@ void spmm_w(const CsrcDev &k, const T *X, T *Y, ColScalars *cols, BlockHeader *h
               "sliced node blocks missing for the block product");
   const bool d16 = k.sell_d16 != nullptr;
   const int grid = std::max(1, std::min((k.nslices + SPC - 1) / SPC, k.max_grid));
-  // FP32: three slot groups' matrix loads per step; FP64 (FP64-pipe
-  // bound): one
-  const int u = k.spmm_unroll > 0 ? k.spmm_unroll : (sizeof(T) == 4 ? 3 : 1);
+  // slot groups of matrix loads per step: ELX_SPMM_UNROLL, else the
+  // autotuner's choice for this width, else three in FP32 and one in FP64
+  // (FP64-pipe bound)
+  constexpr int wi = W == 1 ? 0 : W == 2 ? 1 : W == 4 ? 2 : W == 8 ? 3 : 4;
+  const int tuned = sizeof(T) == 4 ? k.spmm_unroll_w32[wi] : k.spmm_unroll_w64[wi];
+  const int u = k.spmm_unroll > 0 ? k.spmm_unroll : tuned > 0 ? tuned : (sizeof(T) == 4 ? 3 : 1);
 #define ELX_SPMM(B_, DOT_, U_, LD_, D16_)                                                  \
   do {                                                                                      \
     sell_spmm_kernel<T, B_, W, DOT_, false, U_, LD_, D16_><<<grid, kThreads, 0, st>>>(      \

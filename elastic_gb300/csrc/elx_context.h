@@ -75,6 +75,9 @@ struct elx_ctx {
       bk_part, bk_cnt, bk_diag, bk_colmajor;
   int blk_cap = 0;
   int tuned_width[2] = {0, 0};  // autotuned block width (FP64, mixed)
+  // autotuned slot groups in flight of the block product per width
+  // ([FP64, mixed][log2 W]; 0: the default)
+  int tuned_unroll[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
   cudaGraphExec_t block_graph = nullptr;
   int block_graph_w = 0;
   bool block_graph_mixed = false;
@@ -160,6 +163,10 @@ struct elx_ctx {
     k.gather_blocks = gather_blocks;
     k.max_grid = elx::grid_cap(8);
     k.spmm_unroll = spmm_unroll;
+    for (int i = 0; i < 5; i++) {
+      k.spmm_unroll_w64[i] = tuned_unroll[0][i];
+      k.spmm_unroll_w32[i] = tuned_unroll[1][i];
+    }
     if (use_blocks) {
       k.bsize = s.bsize; k.nb = s.nb; k.nnzb = s.nnzb;
       k.bia = bia.as<int32_t>(); k.bt = bt.as<int32_t>();

@@ -196,6 +196,10 @@ struct CsrcDev {
   bool sell64_stream = true;     // streaming loads of the FP64 copy
   // slot groups whose loads the block product issues together (0: default)
   int32_t spmm_unroll = 0;
+  // the autotuner's slot groups in flight per block width (index log2 W;
+  // 0: the default), for the FP32 and the FP64 block products
+  int32_t spmm_unroll_w32[5] = {0, 0, 0, 0, 0};
+  int32_t spmm_unroll_w64[5] = {0, 0, 0, 0, 0};
   // grid bound of the products with fused dots: eight CTAs per SM (the
   // partial sums hold one row per CTA)
   int32_t max_grid = 1;

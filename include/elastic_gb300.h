@@ -208,6 +208,11 @@ int elx_solve_block_device(elx_ctx *ctx, int32_t nrhs, int32_t precision, double
  * (nullable, 5 entries) gets the product times of widths 1, 2, 4, 8, 16 and
  * forces a new measurement. */
 int elx_autotune_block(elx_ctx *ctx, int32_t precision, int32_t *width, double *times_us);
+/* The tiling the autotuner chose for the block product of each width
+ * (unroll[i] for W = 2^i, 5 entries): the slot groups of matrix loads kept in
+ * flight (1-3; 0 = not tuned, the library's default).  No reference
+ * counterpart (the reference has no block product). */
+int elx_block_tiling(elx_ctx *ctx, int32_t precision, int32_t *unroll);
 
 /* ---- solve server ----------------------------------------------------- */
 /* A request loop over many meshes at once (no reference counterpart: the

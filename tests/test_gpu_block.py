@@ -127,3 +127,31 @@ def test_mixed_falls_back_to_fp64_on_ill_conditioned_2d(gpu_ctx):
         assert rel_inf(X64[:, c], Xm[:, c]) <= bar
     assert i1["status"] == 0 and i1["norm_m_r"] <= 3.16 * i1["conv"]
     assert rel_inf(X64[:, 0], x1) <= (1e-10 if i1["refinements"] == -1 else 1e-6)
+
+
+@pytest.mark.parametrize("precision", [E.PREC_MIXED, E.PREC_FP64])
+def test_autotuned_tiling_gives_the_same_bits(built_lib, monkeypatch, precision):
+    """The autotuner picks, per width, how many slot groups of matrix loads
+    the block product keeps in flight (1-3 on 3x3 node blocks).  Each row's
+    sums run in the block order whatever that number, so every tiling gives
+    the same bits: the autotuned solve equals solves with the tiling fixed
+    to 1 and to 3 (ELX_SPMM_UNROLL)."""
+    m = M.box_hexa8(9, 8, 7, jitter=0.2, seed=5)
+    results = []
+    for fixed in (None, "1", "3"):
+        if fixed is None:
+            monkeypatch.delenv("ELX_SPMM_UNROLL", raising=False)
+        else:
+            monkeypatch.setenv("ELX_SPMM_UNROLL", fixed)
+        with E.Context(device=0) as ctx:
+            _, _, _, B = _system(ctx, m, 6)
+            w, _ = ctx.autotune_block(precision, remeasure=True)
+            tiling = ctx.block_tiling(precision)
+            if fixed is None:
+                assert all(1 <= u <= 3 for u in tiling), tiling
+            else:
+                assert tiling == [0] * 5  # a fixed tiling is not tuned
+            X, infos = ctx.solve_block(B, precision=precision, tol=1e-10, width=8)
+            assert all(i["status"] == 0 for i in infos)
+            results.append(X)
+    assert np.array_equal(results[0], results[1]) and np.array_equal(results[0], results[2])
