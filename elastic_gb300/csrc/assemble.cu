@@ -574,7 +574,12 @@ hexa8_team_kernel(MeshDev m, CsrcDev k, int begin, int end, const double *__rest
     sfirst[le][lane] = f;
   }
   __syncthreads();
-  const bool with_u = u != nullptr;
+  // K u only where the element has a non-zero displacement (an element with
+  // u = 0 adds nothing to b; the first solvm pass has u = 0 away from
+  // prescribed values): decided per team, from its 8 lanes' nodes
+  const unsigned team_mask = 0xffu << (threadIdx.x & 24);
+  const bool nz = su[le][lane][0] != 0.0 || su[le][lane][1] != 0.0 || su[le][lane][2] != 0.0;
+  const bool with_u = u != nullptr && (__ballot_sync(0xffffffffu, nz) & team_mask) != 0u;
   double p[8][3];
 #pragma unroll
   for (int a = 0; a < 8; a++)
@@ -643,13 +648,14 @@ hexa8_team_kernel(MeshDev m, CsrcDev k, int begin, int end, const double *__rest
     }
   }
   if (!with_u || b == nullptr) return;
-  // K u over the team: fixed shuffle tree within the 8 lanes
+  // K u over the team: fixed shuffle tree within the team's 8 lanes (other
+  // teams of the warp may have left above)
 #pragma unroll
   for (int off = 4; off > 0; off >>= 1)
 #pragma unroll
     for (int a = 0; a < 8; a++)
 #pragma unroll
-      for (int d = 0; d < 3; d++) p[a][d] += __shfl_xor_sync(0xffffffffu, p[a][d], off, 8);
+      for (int d = 0; d < 3; d++) p[a][d] += __shfl_xor_sync(team_mask, p[a][d], off, 8);
   if (!active) return;
 #pragma unroll
   for (int a = 0; a < 8; a++)
