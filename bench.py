@@ -668,9 +668,10 @@ def run_serve(args):
     n = args.requests
     reqs = [M.serving_request(rng, dof_max=args.max_dof) for _ in range(n)]
     cases = sum(F.shape[0] for _, F in reqs)
-    # ---- sequential plain FP64 (service time per request, back to back)
+    # ---- sequential plain FP64 (service time per request, back to back);
+    # with --rate the arrival rate is given and this half is left out
     service, ref_u = [], {}
-    for i, (m, F) in enumerate(reqs):
+    for i, (m, F) in enumerate(reqs if not getattr(args, "rate", None) else []):
         t0 = time.perf_counter()
         ctx = E.Context(device=0)
         ctx.set_mesh(m)
@@ -691,7 +692,7 @@ def run_serve(args):
         service.append(time.perf_counter() - t0)
         if us:
             ref_u[i] = np.array(us)
-    rate = 1.5 / statistics.mean(service)
+    rate = args.rate if getattr(args, "rate", None) else 1.5 / statistics.mean(service)
     arrivals = np.cumsum(np.random.default_rng(7).exponential(1.0 / rate, n))
     arrivals -= arrivals[0]
     t, lat_seq = 0.0, []
@@ -724,6 +725,7 @@ def run_serve(args):
         done_at.append(t_sub - t_start + latency)
         if i in ref_u:
             errs.append(float(np.abs(U - ref_u[i]).max() / max(np.abs(ref_u[i]).max(), 1e-300)))
+        if i % 8 == 0:
             served_u[i] = U
     th.join()
     stats = srv.stats()
@@ -743,7 +745,7 @@ def run_serve(args):
     import oracle as O
     nth = len(os.sched_getaffinity(0))
     err_o = {"fp64_packed": [], "block": []}
-    for i in sorted(served_u):
+    for i in sorted(served_u) if not getattr(args, "quick", False) else []:
         m, F = reqs[i]
         if m.nnode * m.ndf > 3e5:
             continue
@@ -769,11 +771,13 @@ def run_serve(args):
                        "peak_device_bytes": stats["peak_bytes"],
                        "peak_load_cases_in_pack": stats["peak_slots"],
                        "packed_iterations": stats["iterations"],
+                       "phases_mean_s": {k: stats[f"{k}_phases_mean_s"]
+                                         for k in ("packed", "block")},
                        "all_at_once_solves_per_s": cases / sat_span if sat_span else None},
             "sequential_fp64": {"solves_per_s": cases / seq_span, "requests_per_s": n / seq_span,
                                 "p50_latency_s": pct(lat_seq, 50),
                                 "p99_latency_s": pct(lat_seq, 99), "span_s": seq_span,
-                                "mean_service_s": statistics.mean(service)},
+                                "mean_service_s": statistics.mean(service)} if service else None,
             "max_rel_diff_vs_sequential_sample": max(errs) if errs else None,
             "vs_oracle_fp64": {
                 "requests": sum(1 for i in served_u if reqs[i][0].nnode * reqs[i][0].ndf <= 3e5),
@@ -899,6 +903,12 @@ def main():
                          "48^3 TETRA4 mesh; serve: the served request stream")
     ap.add_argument("--requests", type=int, default=512, help="serve: requests in the stream")
     ap.add_argument("--max-dof", type=float, default=2e6, help="serve: largest request")
+    ap.add_argument("--rate", type=float, default=None,
+                    help="serve: arrival rate in requests/s (leaves out the sequential "
+                         "FP64 half, whose mean service time sets the rate otherwise)")
+    ap.add_argument("--quick", action="store_true",
+                    help="serve: the open stream only (no all-at-once submission of the same "
+                         "requests, no oracle check of the served results)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64",
                     help="solver precision (mixed: FP32 inner PCG + FP64 refinement)")
     args = ap.parse_args()
@@ -918,7 +928,7 @@ def main():
         elif args.mode == "tetra":
             out = run_tetra(args)
         elif args.mode == "serve":
-            args.all_at_once = True
+            args.all_at_once = not args.quick
             out = run_serve(args)
         else:
             out = run_ours(args, dist)

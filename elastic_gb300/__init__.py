@@ -73,10 +73,19 @@ class ServerOpts(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("peak_bytes", C.c_int64),
                 ("resident_bytes", C.c_int64), ("peak_slots", C.c_int64),
-                ("iterations", C.c_int64), ("large_solved", C.c_int64)]
+                ("iterations", C.c_int64), ("large_solved", C.c_int64),
+                ("phase_n", C.c_int64 * 2), ("phase_s", (C.c_double * 5) * 2)]
+    PHASES = ("prepare", "wait_admission", "admit", "wait_start", "solve")
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_[:7]}
+        # mean seconds per phase of the finished packed / block requests
+        for k, kind in enumerate(("packed", "block")):
+            n = self.phase_n[k]
+            d[f"{kind}_phases_mean_s"] = {
+                p: (self.phase_s[k][i] / n if n else None) for i, p in enumerate(self.PHASES)}
+            d[f"{kind}_finished"] = n
+        return d
 
 
 _lib = None

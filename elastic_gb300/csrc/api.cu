@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "elx_context.h"
 
@@ -622,7 +623,7 @@ void gmres64(elx_ctx *c, int kdim, double tol, int maxit, elx_info *info) {
   elx::GmresState init{};
   init.tol = tol;
   init.maxit = maxit;
-  ELX_CUDA(cudaMemcpy(gs, &init, sizeof(init), cudaMemcpyHostToDevice));
+  ELX_CUDA(cudaMemcpyAsync(gs, &init, sizeof(init), cudaMemcpyHostToDevice, c->stream));
   ELX_CUDA(cudaMemsetAsync(c->garrays.p, 0, c->garrays.bytes, c->stream));
   elx::launch_gmres_init(c->s.neq, c->b.as<double>(), c->m.as<double>(), c->xs.as<double>(),
                          c->gbasis.as<double>(), gs, c->partials.as<double>(),
@@ -1019,6 +1020,77 @@ void build_host_structure(const elx::Mesh &m, const int32_t *bc, bool reorder,
 
 }  // namespace elx_api
 
+namespace elx {
+namespace {
+constexpr int kPoolDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kPoolDevices];
+bool g_pool_probed[kPoolDevices];
+int g_pool_users[kPoolDevices];
+std::mutex g_pinned_mu;
+std::vector<void *> g_pinned_free;
+}  // namespace
+
+cudaMemPool_t device_pool(int device) {
+  if (device < 0 || device >= kPoolDevices) return nullptr;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pool_probed[device]) {
+    g_pool_probed[device] = true;
+    const char *env = std::getenv("ELX_DEVICE_POOL");
+    int ok = 0;
+    if (!(env && std::atoi(env) == 0) &&
+        cudaDeviceGetAttribute(&ok, cudaDevAttrMemoryPoolsSupported, device) == cudaSuccess &&
+        ok) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = device;
+      cudaMemPool_t p = nullptr;
+      if (cudaMemPoolCreate(&p, &props) == cudaSuccess) {
+        // freed memory stays reserved for the next allocation (returned
+        // when the last pool user goes, pool_users)
+        uint64_t keep = UINT64_MAX;
+        if (cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep) == cudaSuccess)
+          g_pool[device] = p;
+        else
+          cudaMemPoolDestroy(p);
+      }
+    }
+    (void)cudaGetLastError();
+  }
+  return g_pool[device];
+}
+
+void pool_users(int device, int delta) {
+  if (device < 0 || device >= kPoolDevices) return;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  g_pool_users[device] += delta;
+  if (g_pool_users[device] == 0 && g_pool[device]) cudaMemPoolTrimTo(g_pool[device], 0);
+}
+
+void *pinned_block_get() {
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  if (g_pinned_free.empty()) {
+    constexpr int kPerChunk = 64;
+    void *chunk = nullptr;
+    ELX_CUDA(cudaHostAlloc(&chunk, kPinnedBlock * kPerChunk, cudaHostAllocPortable));
+    for (int i = kPerChunk - 1; i >= 0; i--)
+      g_pinned_free.push_back(static_cast<char *>(chunk) + (size_t)i * kPinnedBlock);
+  }
+  void *p = g_pinned_free.back();
+  g_pinned_free.pop_back();
+  std::memset(p, 0, kPinnedBlock);
+  return p;
+}
+
+void pinned_block_put(void *p) {
+  if (!p) return;
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  g_pinned_free.push_back(p);
+}
+}  // namespace elx
+
 using namespace elx_api;
 
 extern "C" {
@@ -1054,9 +1126,19 @@ int elx_create(elx_ctx **out, const elx_opts *opts) {
     ELX_CUDA(cudaGetDeviceCount(&ndev));
     require(c->device >= 0 && c->device < ndev, ELX_ERR_ARG, "no such CUDA device");
     ELX_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-    ELX_CUDA(cudaHostAlloc(&c->h_scal, 2 * sizeof(elx::PcgScalars), cudaHostAllocDefault));
-    ELX_CUDA(cudaHostAlloc(&c->h_diag, 8 * sizeof(double), cudaHostAllocDefault));
-    ELX_CUDA(cudaHostAlloc(&c->h_flags, 4 * sizeof(int32_t), cudaHostAllocDefault));
+    c->pool = elx::device_pool(c->device);
+    elx::pool_users(c->device, 1);
+    c->pool_user = true;
+    // h_scal (2 PcgScalars), h_diag (8 doubles), h_flags (4 ints) in one
+    // recycled pinned block
+    static_assert(2 * sizeof(elx::PcgScalars) + 8 * sizeof(double) + 4 * sizeof(int32_t) <=
+                      elx::kPinnedBlock,
+                  "pinned block too small");
+    c->pinned = elx::pinned_block_get();
+    char *pb = static_cast<char *>(c->pinned);
+    c->h_scal = reinterpret_cast<elx::PcgScalars *>(pb);
+    c->h_diag = reinterpret_cast<double *>(pb + 2 * sizeof(elx::PcgScalars));
+    c->h_flags = reinterpret_cast<int32_t *>(pb + 2 * sizeof(elx::PcgScalars) + 8 * sizeof(double));
     for (auto &e : c->ev) ELX_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto &e : c->ev_t) ELX_CUDA(cudaEventCreate(&e));
   });
@@ -1093,11 +1175,11 @@ void elx_destroy(elx_ctx *c) {
   for (auto &e : c->ev_t)
     if (e) cudaEventDestroy(e);
   release_block(c);
-  if (c->h_scal) cudaFreeHost(c->h_scal);
-  if (c->h_diag) cudaFreeHost(c->h_diag);
-  if (c->h_flags) cudaFreeHost(c->h_flags);
+  if (c->stream) cudaStreamSynchronize(c->stream);  // the stream-ordered frees
+  elx::pinned_block_put(c->pinned);
   if (c->vtk_host) cudaFreeHost(c->vtk_host);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->pool_user) elx::pool_users(c->device, -1);
   delete c;
 }
 

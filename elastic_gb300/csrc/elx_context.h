@@ -15,6 +15,9 @@ struct elx_ctx {
   int device = 0;
   int verbose = 0;
   cudaStream_t stream = nullptr;
+  cudaMemPool_t pool = nullptr;  // the device's stream-ordered pool (or plain cudaMalloc)
+  void *pinned = nullptr;        // the recycled pinned block of h_scal, h_diag, h_flags
+  bool pool_user = false;        // counted among the pool's users
   int64_t budget = 0, used = 0;
   std::string err;
 
@@ -105,7 +108,8 @@ struct elx_ctx {
     if (budget > 0 && used + (int64_t)bytes > budget)
       throw Error{ELX_ERR_OOM, "HBM budget exceeded: need " + std::to_string(bytes) +
                                    " more bytes, " + std::to_string(budget - used) + " left"};
-    const cudaError_t me = cudaMalloc(&d.p, bytes);
+    const cudaError_t me =
+        pool ? cudaMallocFromPoolAsync(&d.p, bytes, pool, stream) : cudaMalloc(&d.p, bytes);
     if (me != cudaSuccess) {
       d.p = nullptr;
       (void)cudaGetLastError();
@@ -116,7 +120,12 @@ struct elx_ctx {
   }
   void release(DBuf &d) {
     if (d.p) {
-      cudaFree(d.p);
+      // stream-ordered: the memory returns to the pool once the context's
+      // stream has passed its last use
+      if (pool)
+        cudaFreeAsync(d.p, stream);
+      else
+        cudaFree(d.p);
       used -= (int64_t)d.bytes;
     }
     d.p = nullptr;

@@ -126,6 +126,23 @@ constexpr int kSliceRows = 32;
 
 // Streaming multiprocessors of the current device (read once per device).
 int sm_count();
+
+// Device memory of the contexts: one stream-ordered pool per device
+// (cudaMallocFromPoolAsync / cudaFreeAsync on the context's stream), so
+// that a context's allocations and frees wait for its own stream only --
+// cudaFree waits for the whole device, which stalls every other context
+// (a solve server's admissions behind its large solves).  Freed memory
+// stays in the pool for the next allocation while a pool user (a context
+// or a server) lives; the last one to go returns it to the device.
+// nullptr where the device has no memory pools (plain cudaMalloc then).
+cudaMemPool_t device_pool(int device);
+void pool_users(int device, int delta);
+// A context's small pinned host scalars: blocks of kPinnedBlock bytes,
+// carved from larger pinned allocations and recycled, so that creating and
+// destroying contexts pins and unpins no memory once warm.
+constexpr size_t kPinnedBlock = 1024;
+void *pinned_block_get();
+void pinned_block_put(void *p);
 // Grid bound of the grid-stride kernels: per_sm CTAs on every SM.
 inline int grid_cap(int per_sm) { return sm_count() * per_sm; }
 

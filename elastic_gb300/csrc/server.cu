@@ -29,6 +29,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -252,7 +253,10 @@ struct SrvRequest {
   std::vector<double> f;  // nrhs x (ndf x nnode)
   double tol = 1e-8;
   int maxit = 10000;
-  double t_submit = 0, t_done = 0;
+  // submitted, prepared (host structure built), admission started and done
+  // (device memory, uploads, assembly), solve started (joined the pack or
+  // the block solve began), done
+  double t_submit = 0, t_prepared = 0, t_admit0 = 0, t_admitted = 0, t_start = 0, t_done = 0;
   // host preparation
   elx::Structure s;
   std::vector<double> b0;  // nrhs x neq
@@ -290,7 +294,8 @@ struct elx_server {
   int64_t next_ticket = 1;
   bool stopping = false;
   std::vector<std::thread> prep_threads, large_threads;
-  std::thread admit_thread, loop_thread;
+  std::vector<std::thread> admit_threads;
+  std::thread loop_thread;
   std::condition_variable cv_large;
   std::deque<std::shared_ptr<SrvRequest>> large_ready;
   std::string fatal;
@@ -314,6 +319,9 @@ struct elx_server {
   // statistics
   std::atomic<int64_t> submitted{0}, completed{0}, peak_used{0}, peak_slots{0}, iterations{0},
       large_solved{0};
+  bool pool_user = false;     // holds the device pool's memory while it lives
+  double phase_s[2][5] = {};  // under mu: per-phase seconds of finished requests
+  int64_t phase_n[2] = {};    // (packed, block) and their count
 };
 
 namespace {
@@ -386,6 +394,13 @@ void finish(elx_server *sv, const std::shared_ptr<SrvRequest> &q) {
   {
     std::lock_guard<std::mutex> lk(sv->mu);
     if (q->t_done == 0) q->t_done = now_s();
+    if (q->status == ELX_OK && q->t_start > 0) {
+      const int k = q->large ? 1 : 0;
+      const double t[6] = {q->t_submit, q->t_prepared, q->t_admit0, q->t_admitted, q->t_start,
+                           q->t_done};
+      for (int i = 0; i < 5; i++) sv->phase_s[k][i] += t[i + 1] - t[i];
+      sv->phase_n[k]++;
+    }
     q->done = true;
     q->mesh = elx::Mesh{};
     q->s = elx::Structure{};
@@ -410,6 +425,7 @@ void prep_worker(elx_server *sv) {
       prep_request(*q);
       q->large = sv->large_mode >= 0 && q->s.neq >= sv->large_dofs;
       q->need_bytes = estimate_bytes(*q);
+      q->t_prepared = now_s();
       std::lock_guard<std::mutex> lk(sv->mu);
       sv->prepared.push_back(q);
     } catch (const Error &e) {
@@ -586,7 +602,9 @@ void admit_loop(elx_server *sv) {
         continue;
       }
       try {
+        q->t_admit0 = now_s();
         admit(sv, *q);
+        q->t_admitted = now_s();
         {
           std::lock_guard<std::mutex> lk(sv->mu);
           (q->large ? sv->large_ready : sv->joinable).push_back(q);
@@ -624,6 +642,7 @@ void large_loop(elx_server *sv) {
       sv->large_ready.pop_front();
     }
     try {
+      q->t_start = now_s();
       ELX_CUDA(cudaSetDevice(sv->device));
       elx_ctx *c = q->ctx;
       const size_t n = (size_t)c->s.neq;
@@ -685,6 +704,7 @@ void gpu_loop(elx_server *sv) {
           sv->cv_admit.wait(lk, [&] { return sv->stopping || !sv->joinable.empty(); });
         if (sv->stopping) return;
         while (!sv->joinable.empty()) {
+          sv->joinable.front()->t_start = now_s();
           sv->active.push_back(sv->joinable.front());
           sv->joinable.pop_front();
           repack = true;
@@ -801,6 +821,12 @@ int elx_server_create(elx_server **out, const elx_server_opts *opts) {
   }
   const cudaError_t e1 = cudaSetDevice(sv->device);
   cudaError_t e = e1;
+  if (e == cudaSuccess) {
+    // the request contexts' memory stays in the device pool between requests
+    elx::device_pool(sv->device);
+    elx::pool_users(sv->device, 1);
+    sv->pool_user = true;
+  }
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&sv->d_sc, sizeof(SlotScalars) * sv->max_slots);
   if (e == cudaSuccess) e = cudaMemset(sv->d_sc, 0, sizeof(SlotScalars) * sv->max_slots);
@@ -817,7 +843,11 @@ int elx_server_create(elx_server **out, const elx_server_opts *opts) {
   }
   for (int i = sv->max_slots - 1; i >= 0; i--) sv->slot_free.push_back(i);
   for (int i = 0; i < nthreads; i++) sv->prep_threads.emplace_back(prep_worker, sv);
-  sv->admit_thread = std::thread(admit_loop, sv);
+  // admissions (uploads, assembly) of several requests at once, each on its
+  // own context's stream, taken from the prepared queue in arrival order
+  const char *adm_env = std::getenv("ELX_SERVER_ADMIT_THREADS");
+  const int nadmit = adm_env && std::atoi(adm_env) > 0 ? std::atoi(adm_env) : 2;
+  for (int i = 0; i < nadmit; i++) sv->admit_threads.emplace_back(admit_loop, sv);
   for (int i = 0; i < nlarge; i++) sv->large_threads.emplace_back(large_loop, sv);
   sv->loop_thread = std::thread(gpu_loop, sv);
   *out = sv;
@@ -838,13 +868,17 @@ void elx_server_destroy(elx_server *sv) {
     if (t.joinable()) t.join();
   for (auto &t : sv->large_threads)
     if (t.joinable()) t.join();
-  if (sv->admit_thread.joinable()) sv->admit_thread.join();
+  for (auto &t : sv->admit_threads)
+    if (t.joinable()) t.join();
   if (sv->loop_thread.joinable()) sv->loop_thread.join();
   cudaSetDevice(sv->device);
+  // the pack's last launches (a loop that stopped on an error) end before
+  // the requests' memory goes back: their frees are ordered on the request
+  // streams only
+  if (sv->stream) cudaStreamSynchronize(sv->stream);
   for (auto &q : sv->active) release_request(sv, *q);
   for (auto &q : sv->joinable) release_request(sv, *q);
   for (auto &q : sv->large_ready) release_request(sv, *q);
-  if (sv->stream) cudaStreamSynchronize(sv->stream);
   if (sv->d_sc) cudaFree(sv->d_sc);
   if (sv->d_desc) cudaFree(sv->d_desc);
   if (sv->d_part) cudaFree(sv->d_part);
@@ -852,6 +886,7 @@ void elx_server_destroy(elx_server *sv) {
   if (sv->h_desc) cudaFreeHost(sv->h_desc);
   if (sv->ev_poll) cudaEventDestroy(sv->ev_poll);
   if (sv->stream) cudaStreamDestroy(sv->stream);
+  if (sv->pool_user) elx::pool_users(sv->device, -1);
   delete sv;
 }
 
@@ -928,6 +963,10 @@ int elx_server_get_stats(elx_server *sv, elx_server_stats *st) {
   {
     std::lock_guard<std::mutex> lk(sv->mu);
     st->resident_bytes = sv->used;
+    for (int k = 0; k < 2; k++) {
+      st->phase_n[k] = sv->phase_n[k];
+      for (int i = 0; i < 5; i++) st->phase_s[k][i] = sv->phase_s[k][i];
+    }
   }
   return sv->fatal.empty() ? ELX_OK : ELX_ERR_CUDA;
 }

@@ -248,6 +248,12 @@ typedef struct elx_server_stats {
   int64_t peak_slots;     /* most load cases in one packed iteration         */
   int64_t iterations;     /* packed iterations run                           */
   int64_t large_solved;   /* requests solved whole (block PCG)               */
+  /* [0] packed, [1] block: finished requests and their summed seconds from
+   * submit to prepared (host structure), to admission start (waiting for
+   * memory / slots), to admitted (uploads, assembly, preconditioner), to
+   * the solve's start (joining the pack / a block-solve thread), to done */
+  int64_t phase_n[2];
+  double phase_s[2][5];
 } elx_server_stats;
 int elx_server_create(elx_server **out, const elx_server_opts *opts);
 /* Queues a request (the arrays are copied): a mesh as for elx_set_mesh,
