@@ -701,7 +701,8 @@ def run_serve(args):
         lat_seq.append(t - a)
     seq_span = t
     # ---- served
-    srv = E.Server(device=0, hbm_budget=int(150e9), prep_threads=len(os.sched_getaffinity(0)))
+    srv = E.Server(device=0, hbm_budget=int(150e9), prep_threads=len(os.sched_getaffinity(0)),
+                   large_workers=getattr(args, "large_workers", 0))
     tickets = [None] * n
     t_start = time.perf_counter() + 0.5
 
@@ -906,6 +907,8 @@ def main():
     ap.add_argument("--rate", type=float, default=None,
                     help="serve: arrival rate in requests/s (leaves out the sequential "
                          "FP64 half, whose mean service time sets the rate otherwise)")
+    ap.add_argument("--large-workers", type=int, default=0,
+                    help="serve: block-solve worker threads (0: the server's default, 2)")
     ap.add_argument("--quick", action="store_true",
                     help="serve: the open stream only (no all-at-once submission of the same "
                          "requests, no oracle check of the served results)")

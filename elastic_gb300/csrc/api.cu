@@ -854,7 +854,17 @@ void solve_block(elx_ctx *c, int nrhs, int precision, double tol, int maxit, int
     // batches of kBatch iterations until no column is active
     elx::BlockHeader hh{};
     const int max_batches = maxit / kBatch + 2;
+    struct Gate {  // batch_gate(0) also when a launch or the poll throws
+      elx_ctx *c;
+      explicit Gate(elx_ctx *cc) : c(cc) {
+        if (c->batch_gate) c->batch_gate(c->batch_gate_user, 1);
+      }
+      ~Gate() {
+        if (c->batch_gate) c->batch_gate(c->batch_gate_user, 0);
+      }
+    };
     for (int bt = 0; bt < max_batches; bt++) {
+      Gate gate(c);
       ELX_CUDA(cudaGraphLaunch(c->block_graph, c->stream));
       c->launches += (int64_t)(per_iter * kBatch + 0.5);
       ELX_CUDA(cudaMemcpyAsync(&hh, v.hdr, sizeof(hh), cudaMemcpyDeviceToHost, c->stream));

@@ -82,6 +82,11 @@ struct elx_ctx {
   // ([FP64, mixed][log2 W]; 0: the default)
   int tuned_unroll[2][5] = {{0, 0, 0, 0, 0}, {0, 0, 0, 0, 0}};
   cudaGraphExec_t block_graph = nullptr;
+  // called with 1 before and 0 after each batch of block iterations (launch
+  // and poll); a solve server holds a block solve's batches back here while
+  // small requests need the GPU
+  void (*batch_gate)(void *user, int enter) = nullptr;
+  void *batch_gate_user = nullptr;
   int block_graph_w = 0;
   bool block_graph_mixed = false;
   // scalars, partials, counters, flags

@@ -264,6 +264,7 @@ struct SrvRequest {
   int64_t charged = 0;  // bytes counted against the budget while resident
   bool counted = false;
   bool large = false;   // solved whole on its own stream (block PCG), not packed
+  bool small_counted = false;  // counted in the server's small_busy
   // device state
   elx_ctx *ctx = nullptr;
   DBuf vecs;  // b (nrhs x neq), then per load case x, r, p, q
@@ -320,6 +321,19 @@ struct elx_server {
   std::atomic<int64_t> submitted{0}, completed{0}, peak_used{0}, peak_slots{0}, iterations{0},
       large_solved{0};
   bool pool_user = false;     // holds the device pool's memory while it lives
+  // stream priority of the pack and of the packed requests' admissions (the
+  // device's greatest; the block solves keep the default, its least), or 0
+  // when ELX_SERVER_PRIORITY=0
+  int prio_hi = 0;
+  // batch gate of the block solves: while small requests are being admitted
+  // or iterate in the pack (small_busy > 0), one block solve runs its
+  // iteration batches at a time; otherwise all nlarge workers do
+  // (ELX_SERVER_GATE=0: no gate)
+  bool gate_on = true;
+  int nlarge = 2;
+  std::mutex gate_mu;
+  std::condition_variable cv_gate;
+  int small_busy = 0, gate_running = 0;
   double phase_s[2][5] = {};  // under mu: per-phase seconds of finished requests
   int64_t phase_n[2] = {};    // (packed, block) and their count
 };
@@ -443,10 +457,38 @@ void prep_worker(elx_server *sv) {
   }
 }
 
+// The block solves' batch gate (elx_ctx::batch_gate of large requests).
+// A waiting batch is held back only while another one runs, and every
+// batch ends, so the wait ends.
+void block_gate(void *user, int enter) {
+  auto *sv = static_cast<elx_server *>(user);
+  std::unique_lock<std::mutex> lk(sv->gate_mu);
+  if (enter) {
+    sv->cv_gate.wait(lk, [&] {
+      return sv->gate_running < (sv->small_busy > 0 ? 1 : sv->nlarge);
+    });
+    sv->gate_running++;
+  } else {
+    sv->gate_running--;
+    lk.unlock();
+    sv->cv_gate.notify_all();
+  }
+}
+
+void small_busy_add(elx_server *sv, int delta) {
+  {
+    std::lock_guard<std::mutex> lk(sv->gate_mu);
+    sv->small_busy += delta;
+  }
+  if (delta < 0) sv->cv_gate.notify_all();
+}
+
 // Frees a request's device state, slots and budget share.
 void release_request(elx_server *sv, SrvRequest &q) {
   if (q.ready) cudaEventDestroy(q.ready);
   q.ready = nullptr;
+  if (q.small_counted) small_busy_add(sv, -1);
+  q.small_counted = false;
   if (q.ctx) {
     q.ctx->release(q.vecs);
     elx_destroy(q.ctx);
@@ -472,6 +514,17 @@ void admit(elx_server *sv, SrvRequest &q) {
   int st = elx_create(&q.ctx, &o);
   if (st != ELX_OK) throw Error{st, "context creation failed"};
   elx_ctx *c = q.ctx;
+  if (q.large && sv->gate_on) {
+    c->batch_gate = block_gate;
+    c->batch_gate_user = sv;
+  }
+  if (!q.large && sv->prio_hi != 0) {
+    // a small request's uploads, assembly and slot starts ahead of the block
+    // solves (nothing is queued on the context's stream yet)
+    ELX_CUDA(cudaStreamDestroy(c->stream));
+    c->stream = nullptr;
+    ELX_CUDA(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, sv->prio_hi));
+  }
   c->mesh = std::move(q.mesh);
   c->s = std::move(q.s);
   c->have_mesh = true;
@@ -603,6 +656,10 @@ void admit_loop(elx_server *sv) {
       }
       try {
         q->t_admit0 = now_s();
+        if (!q->large) {
+          small_busy_add(sv, 1);
+          q->small_counted = true;
+        }
         admit(sv, *q);
         q->t_admitted = now_s();
         {
@@ -819,6 +876,9 @@ int elx_server_create(elx_server **out, const elx_server_opts *opts) {
     sv->large_mode = opts->large_mode;
     if (opts->large_workers > 0) nlarge = opts->large_workers;
   }
+  sv->nlarge = nlarge;
+  const char *gate_env = std::getenv("ELX_SERVER_GATE");
+  sv->gate_on = !(gate_env && std::atoi(gate_env) == 0);
   const cudaError_t e1 = cudaSetDevice(sv->device);
   cudaError_t e = e1;
   if (e == cudaSuccess) {
@@ -827,7 +887,12 @@ int elx_server_create(elx_server **out, const elx_server_opts *opts) {
     elx::pool_users(sv->device, 1);
     sv->pool_user = true;
   }
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
+  int least = 0, greatest = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  const char *prio_env = std::getenv("ELX_SERVER_PRIORITY");
+  sv->prio_hi = prio_env && std::atoi(prio_env) == 0 ? 0 : greatest;
+  if (e == cudaSuccess)
+    e = cudaStreamCreateWithPriority(&sv->stream, cudaStreamNonBlocking, sv->prio_hi);
   if (e == cudaSuccess) e = cudaMalloc(&sv->d_sc, sizeof(SlotScalars) * sv->max_slots);
   if (e == cudaSuccess) e = cudaMemset(sv->d_sc, 0, sizeof(SlotScalars) * sv->max_slots);
   if (e == cudaSuccess) e = cudaMalloc(&sv->d_desc, sizeof(SlotDesc) * sv->max_slots);

@@ -122,3 +122,28 @@ def test_large_requests_solved_whole(built_lib, mode, bar):
         for (m, F), (U, _, _, _) in zip(reqs[:3], res[:3]):
             U1, _, _, st1 = srv.wait(srv.submit(m, F, tol=TOL, maxit=50000), timeout=300)
             assert st1 == 0 and np.array_equal(U1, U)
+
+
+def test_phase_statistics(built_lib):
+    """The server times each finished request's phases (structure built,
+    waiting for admission, admitted, waiting to start, solved); they add up
+    to the request's latency, and the counts to the finished requests."""
+    reqs = _requests(13, 8, dof_max=2e5)
+    with E.Server(device=0, large_dofs=50000) as srv:
+        tickets = [srv.submit(m, F, tol=1e-8) for m, F in reqs]
+        res = [srv.wait(t, timeout=300) for t in tickets]
+        assert all(r[3] == 0 for r in res)
+        st = srv.stats()
+    assert st["packed_finished"] + st["block_finished"] == len(reqs)
+    assert st["block_finished"] == st["large_solved"]
+    total = 0.0
+    for kind in ("packed", "block"):
+        n = st[f"{kind}_finished"]
+        if not n:
+            continue
+        ph = st[f"{kind}_phases_mean_s"]
+        assert set(ph) == {"prepare", "wait_admission", "admit", "wait_start", "solve"}
+        assert all(v >= 0 for v in ph.values()) and ph["solve"] > 0 and ph["admit"] > 0
+        total += n * sum(ph.values())
+    lat = sum(r[2] for r in res)
+    assert abs(total - lat) <= 1e-6 * lat, (total, lat)
