@@ -39,6 +39,7 @@
 #include <vector>
 
 #include "elx_context.h"
+#include "elx_gate.h"
 #include "elx_reduce.cuh"
 
 namespace elx {
@@ -264,7 +265,7 @@ struct SrvRequest {
   int64_t charged = 0;  // bytes counted against the budget while resident
   bool counted = false;
   bool large = false;   // solved whole on its own stream (block PCG), not packed
-  bool small_counted = false;  // counted in the server's small_busy
+  bool small_counted = false;  // counted among the gate's small requests
   // device state
   elx_ctx *ctx = nullptr;
   DBuf vecs;  // b (nrhs x neq), then per load case x, r, p, q
@@ -326,14 +327,10 @@ struct elx_server {
   // when ELX_SERVER_PRIORITY=0
   int prio_hi = 0;
   // batch gate of the block solves: while small requests are being admitted
-  // or iterate in the pack (small_busy > 0), one block solve runs its
-  // iteration batches at a time; otherwise all nlarge workers do
-  // (ELX_SERVER_GATE=0: no gate)
+  // or iterate in the pack, one block solve runs its iteration batches at a
+  // time; otherwise all large workers do (ELX_SERVER_GATE=0: no gate)
   bool gate_on = true;
-  int nlarge = 2;
-  std::mutex gate_mu;
-  std::condition_variable cv_gate;
-  int small_busy = 0, gate_running = 0;
+  elx::BatchGate gate;
   double phase_s[2][5] = {};  // under mu: per-phase seconds of finished requests
   int64_t phase_n[2] = {};    // (packed, block) and their count
 };
@@ -458,36 +455,19 @@ void prep_worker(elx_server *sv) {
 }
 
 // The block solves' batch gate (elx_ctx::batch_gate of large requests).
-// A waiting batch is held back only while another one runs, and every
-// batch ends, so the wait ends.
 void block_gate(void *user, int enter) {
   auto *sv = static_cast<elx_server *>(user);
-  std::unique_lock<std::mutex> lk(sv->gate_mu);
-  if (enter) {
-    sv->cv_gate.wait(lk, [&] {
-      return sv->gate_running < (sv->small_busy > 0 ? 1 : sv->nlarge);
-    });
-    sv->gate_running++;
-  } else {
-    sv->gate_running--;
-    lk.unlock();
-    sv->cv_gate.notify_all();
-  }
-}
-
-void small_busy_add(elx_server *sv, int delta) {
-  {
-    std::lock_guard<std::mutex> lk(sv->gate_mu);
-    sv->small_busy += delta;
-  }
-  if (delta < 0) sv->cv_gate.notify_all();
+  if (enter)
+    sv->gate.enter();
+  else
+    sv->gate.leave();
 }
 
 // Frees a request's device state, slots and budget share.
 void release_request(elx_server *sv, SrvRequest &q) {
   if (q.ready) cudaEventDestroy(q.ready);
   q.ready = nullptr;
-  if (q.small_counted) small_busy_add(sv, -1);
+  if (q.small_counted) sv->gate.small(-1);
   q.small_counted = false;
   if (q.ctx) {
     q.ctx->release(q.vecs);
@@ -657,7 +637,7 @@ void admit_loop(elx_server *sv) {
       try {
         q->t_admit0 = now_s();
         if (!q->large) {
-          small_busy_add(sv, 1);
+          sv->gate.small(1);
           q->small_counted = true;
         }
         admit(sv, *q);
@@ -876,7 +856,7 @@ int elx_server_create(elx_server **out, const elx_server_opts *opts) {
     sv->large_mode = opts->large_mode;
     if (opts->large_workers > 0) nlarge = opts->large_workers;
   }
-  sv->nlarge = nlarge;
+  sv->gate.set_workers(nlarge);
   const char *gate_env = std::getenv("ELX_SERVER_GATE");
   sv->gate_on = !(gate_env && std::atoi(gate_env) == 0);
   const cudaError_t e1 = cudaSetDevice(sv->device);
