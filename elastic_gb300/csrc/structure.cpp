@@ -4,6 +4,7 @@
 // arrays: the tiled transposed index of the SpMV, an element colouring and
 // the per-element slot map used by the assembly kernels.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <numeric>
 #include <thread>
@@ -11,6 +12,31 @@
 #include "elx_internal.h"
 
 namespace elx {
+
+namespace {
+
+// Runs f(begin, end) over [0, n) in contiguous chunks on up to 16 threads,
+// with at least min_chunk items per thread (small meshes run on the calling
+// thread alone).  f must not throw.
+template <class F>
+void parallel_chunks(int64_t n, int64_t min_chunk, F &&f) {
+  int64_t nt = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  nt = std::min<int64_t>(nt, n / std::max<int64_t>(1, min_chunk));
+  if (nt <= 1) {
+    if (n > 0) f((int64_t)0, n);
+    return;
+  }
+  const int64_t per = (n + nt - 1) / nt;
+  std::vector<std::thread> th;
+  for (int64_t w = 1; w < nt; w++) {
+    const int64_t b = w * per, e = std::min(n, b + per);
+    if (b < e) th.emplace_back([&f, b, e] { f(b, e); });
+  }
+  f((int64_t)0, std::min(n, per));
+  for (auto &t : th) t.join();
+}
+
+}  // namespace
 
 int elem_nodes(int iel) {
   switch (iel) {
@@ -30,39 +56,51 @@ int elem_nodes(int iel) {
 // Output is 0-based: neighbours of node v are adj[xadj[v] .. xadj[v+1]).
 void node_graph(const Mesh &m, std::vector<int32_t> &xadj, std::vector<int32_t> &adj) {
   const int nen1 = m.nen + 1;
+  // every element's node pairs scattered into per-node lists (elements in
+  // parallel: a list's order depends on the threads, its sorted set does not)
   std::vector<int32_t> cnt(m.nnode + 1, 0);
-  for (int el = 0; el < m.numel; el++)
-    for (int a = 0; a < m.nen; a++) {
-      int no = m.ix[(size_t)el * nen1 + a];
-      if (no <= 0 || no > m.nnode) continue;
-      cnt[no] += m.nen - 1;
-    }
+  parallel_chunks(m.numel, 65536, [&](int64_t e0, int64_t e1) {
+    for (int64_t el = e0; el < e1; el++)
+      for (int a = 0; a < m.nen; a++) {
+        int no = m.ix[(size_t)el * nen1 + a];
+        if (no <= 0 || no > m.nnode) continue;
+        __atomic_fetch_add(&cnt[no], m.nen - 1, __ATOMIC_RELAXED);
+      }
+  });
   std::vector<int64_t> start(m.nnode + 1, 0);
   for (int v = 0; v < m.nnode; v++) start[v + 1] = start[v] + cnt[v + 1];
   std::vector<int32_t> raw(start[m.nnode]);
   std::vector<int64_t> fill(start.begin(), start.end() - 1);
-  for (int el = 0; el < m.numel; el++) {
-    const int32_t *c = &m.ix[(size_t)el * nen1];
-    for (int a = 0; a < m.nen; a++) {
-      int na = c[a];
-      if (na <= 0 || na > m.nnode) continue;
-      for (int b = 0; b < m.nen; b++) {
-        int nb = c[b];
-        if (nb <= 0 || nb > m.nnode || nb == na) continue;
-        raw[fill[na - 1]++] = nb - 1;
+  parallel_chunks(m.numel, 65536, [&](int64_t e0, int64_t e1) {
+    for (int64_t el = e0; el < e1; el++) {
+      const int32_t *c = &m.ix[(size_t)el * nen1];
+      for (int a = 0; a < m.nen; a++) {
+        int na = c[a];
+        if (na <= 0 || na > m.nnode) continue;
+        for (int b = 0; b < m.nen; b++) {
+          int nb = c[b];
+          if (nb <= 0 || nb > m.nnode || nb == na) continue;
+          raw[__atomic_fetch_add(&fill[na - 1], (int64_t)1, __ATOMIC_RELAXED)] = nb - 1;
+        }
       }
     }
-  }
+  });
+  // each node's list sorted and deduplicated in place, then packed
+  std::vector<int32_t> nuniq(m.nnode);
+  parallel_chunks(m.nnode, 8192, [&](int64_t v0, int64_t v1) {
+    for (int64_t v = v0; v < v1; v++) {
+      auto b = raw.begin() + start[v], e = raw.begin() + fill[v];
+      std::sort(b, e);
+      nuniq[v] = (int32_t)(std::unique(b, e) - b);
+    }
+  });
   xadj.assign(m.nnode + 1, 0);
-  adj.clear();
-  adj.reserve(raw.size() / 2 + 1);
-  for (int v = 0; v < m.nnode; v++) {
-    auto b = raw.begin() + start[v], e = raw.begin() + fill[v];
-    std::sort(b, e);
-    auto last = std::unique(b, e);
-    adj.insert(adj.end(), b, last);
-    xadj[v + 1] = (int32_t)adj.size();
-  }
+  for (int v = 0; v < m.nnode; v++) xadj[v + 1] = xadj[v] + nuniq[v];
+  adj.assign(xadj[m.nnode], 0);
+  parallel_chunks(m.nnode, 8192, [&](int64_t v0, int64_t v1) {
+    for (int64_t v = v0; v < v1; v++)
+      std::copy(raw.begin() + start[v], raw.begin() + start[v] + nuniq[v], adj.begin() + xadj[v]);
+  });
 }
 
 namespace {
@@ -233,38 +271,40 @@ void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> 
     nfree[v] = c;
   }
   ia.assign(neq + 1, 0);
-  // row lengths
-  std::vector<int32_t> lower_cols(m.nnode, 0);
-  for (int v = 0; v < m.nnode; v++) {
-    if (!nfree[v]) continue;
-    int32_t cnt = 0;
-    for (int k = xadj[v]; k < xadj[v + 1]; k++) {
-      int w = adj[k];
-      if (nfree[w] && first[w] < first[v]) cnt += nfree[w];
+  // row lengths (each node writes its own rows)
+  parallel_chunks(m.nnode, 8192, [&](int64_t v0, int64_t v1) {
+    for (int64_t v = v0; v < v1; v++) {
+      if (!nfree[v]) continue;
+      int32_t cnt = 0;
+      for (int k = xadj[v]; k < xadj[v + 1]; k++) {
+        int w = adj[k];
+        if (nfree[w] && first[w] < first[v]) cnt += nfree[w];
+      }
+      for (int d = 0; d < nfree[v]; d++) ia[first[v] - 1 + d + 1] = cnt + d;
     }
-    lower_cols[v] = cnt;
-    for (int d = 0; d < nfree[v]; d++) ia[first[v] - 1 + d + 1] = cnt + d;
-  }
+  });
   ia[0] = 1;
   for (int r = 0; r < neq; r++) ia[r + 1] += ia[r];
   ja.assign((size_t)ia[neq] - 1, 0);
-  std::vector<std::pair<int32_t, int32_t>> blocks;
-  for (int v = 0; v < m.nnode; v++) {
-    if (!nfree[v]) continue;
-    blocks.clear();
-    for (int k = xadj[v]; k < xadj[v + 1]; k++) {
-      int w = adj[k];
-      if (nfree[w] && first[w] < first[v]) blocks.emplace_back(first[w], nfree[w]);
+  parallel_chunks(m.nnode, 8192, [&](int64_t v0, int64_t v1) {
+    std::vector<std::pair<int32_t, int32_t>> blocks;
+    for (int64_t v = v0; v < v1; v++) {
+      if (!nfree[v]) continue;
+      blocks.clear();
+      for (int k = xadj[v]; k < xadj[v + 1]; k++) {
+        int w = adj[k];
+        if (nfree[w] && first[w] < first[v]) blocks.emplace_back(first[w], nfree[w]);
+      }
+      std::sort(blocks.begin(), blocks.end());
+      for (int d = 0; d < nfree[v]; d++) {
+        int32_t r = first[v] + d;  // 1-based row
+        int64_t p = ia[r - 1] - 1;
+        for (auto &b : blocks)
+          for (int t = 0; t < b.second; t++) ja[p++] = b.first + t;
+        for (int t = 0; t < d; t++) ja[p++] = first[v] + t;
+      }
     }
-    std::sort(blocks.begin(), blocks.end());
-    for (int d = 0; d < nfree[v]; d++) {
-      int32_t r = first[v] + d;  // 1-based row
-      int64_t p = ia[r - 1] - 1;
-      for (auto &b : blocks)
-        for (int t = 0; t < b.second; t++) ja[p++] = b.first + t;
-      for (int t = 0; t < d; t++) ja[p++] = first[v] + t;
-    }
-  }
+  });
 }
 
 // Greedy element colouring: each element, in element order, takes the
@@ -276,9 +316,9 @@ void csrc_pattern(const Mesh &m, const Structure &s, const std::vector<int32_t> 
 int color_elements(const Mesh &m, std::vector<int32_t> &color) {
   const int nen1 = m.nen + 1;
   color.assign(m.numel, -1);
-  std::vector<std::vector<uint64_t>> used;  // per node, bit per colour (64 per word)
+  // per node a bit per colour taken, `words` 64-bit words per node, node-major
   int words = 1;
-  used.assign(m.nnode, std::vector<uint64_t>(words, 0));
+  std::vector<uint64_t> used((size_t)m.nnode, 0);
   int ncolors = 0;
   for (int el = 0; el < m.numel; el++) {
     const int32_t *c = &m.ix[(size_t)el * nen1];
@@ -286,17 +326,22 @@ int color_elements(const Mesh &m, std::vector<int32_t> &color) {
     int nv = elem_nodes(iel);
     int chosen = -1;
     for (int w = 0; chosen < 0; w++) {
-      if (w == words) {
+      if (w == words) {  // more than 64 * words colours: widen every node's set
+        std::vector<uint64_t> wider((size_t)m.nnode * (words + 1), 0);
+        for (size_t v = 0; v < (size_t)m.nnode; v++)
+          std::copy(used.begin() + v * words, used.begin() + (v + 1) * words,
+                    wider.begin() + v * (words + 1));
+        used.swap(wider);
         words++;
-        for (auto &u : used) u.push_back(0);
       }
       uint64_t busy = 0;
-      for (int a = 0; a < nv; a++) busy |= used[c[a] - 1][w];
+      for (int a = 0; a < nv; a++) busy |= used[(size_t)(c[a] - 1) * words + w];
       if (~busy) chosen = w * 64 + __builtin_ctzll(~busy);
     }
     color[el] = chosen;
     ncolors = std::max(ncolors, chosen + 1);
-    for (int a = 0; a < nv; a++) used[c[a] - 1][chosen / 64] |= 1ull << (chosen % 64);
+    for (int a = 0; a < nv; a++)
+      used[(size_t)(c[a] - 1) * words + chosen / 64] |= 1ull << (chosen % 64);
   }
   return ncolors;
 }
@@ -314,14 +359,20 @@ void derive_structure(const Mesh &m, Structure &s) {
   const int nen1 = m.nen + 1;
   std::vector<int32_t> color;
   s.ncolors = color_elements(m, color);
-  // group by (colour, element type), elements ascending inside a group
-  s.elem_order.resize(m.numel);
-  std::iota(s.elem_order.begin(), s.elem_order.end(), 0);
+  // group by (colour, element type), elements ascending inside a group: a
+  // counting sort on colour * kTypes + type, scattered in element order
   auto type_of = [&](int el) { return m.ie[m.ix[(size_t)el * nen1 + m.nen] - 1]; };
-  std::stable_sort(s.elem_order.begin(), s.elem_order.end(), [&](int a, int b) {
-    if (color[a] != color[b]) return color[a] < color[b];
-    return type_of(a) < type_of(b);
-  });
+  constexpr int kTypes = 8;  // element type codes 2..7
+  std::vector<int64_t> bucket((size_t)s.ncolors * kTypes + 1, 0);
+  for (int el = 0; el < m.numel; el++) {
+    const int t = type_of(el);
+    ELX_REQUIRE(t >= 0 && t < kTypes, ELX_ERR_BAD_ELEMENT, "unsupported element type");
+    bucket[(size_t)color[el] * kTypes + t + 1]++;
+  }
+  for (size_t k = 1; k < bucket.size(); k++) bucket[k] += bucket[k - 1];
+  s.elem_order.resize(m.numel);
+  for (int el = 0; el < m.numel; el++)
+    s.elem_order[bucket[(size_t)color[el] * kTypes + type_of(el)]++] = el;
   s.segments.clear();
   s.color_of_segment.clear();
   for (int i = 0; i < m.numel;) {
@@ -342,27 +393,33 @@ void derive_structure(const Mesh &m, Structure &s) {
       int q = s.id[(size_t)v * m.ndf + d];
       if (q > 0) first[v] = q;  // smallest free equation of the node
     }
-  for (int t = 0; t < m.numel; t++) {
-    int el = s.elem_order[t];
-    const int32_t *c = &m.ix[(size_t)el * nen1];
-    int nv = elem_nodes(type_of(el));
-    int pair = 0;
-    for (int a = 0; a < nen; a++)
-      for (int b = a + 1; b < nen; b++, pair++) {
-        if (a >= nv || b >= nv) continue;
-        int va = c[a] - 1, vb = c[b] - 1;
-        if (!first[va] || !first[vb] || va == vb) continue;
-        int hi = first[va] > first[vb] ? va : vb;
-        int lo = hi == va ? vb : va;
-        int32_t r = first[hi] - 1;  // 0-based row of the higher node's first dof
-        const int32_t *rb = s.ja.data() + (s.ia[r] - 1);
-        const int32_t *re = s.ja.data() + (s.ia[r + 1] - 1);
-        const int32_t *pos = std::lower_bound(rb, re, first[lo]);
-        ELX_REQUIRE(pos != re && *pos == first[lo], ELX_ERR_ARG,
-                    "CSRC pattern does not contain an element's node pair");
-        s.slot[(size_t)pair * m.numel + t] = (int32_t)(pos - rb);
-      }
-  }
+  std::atomic<bool> missing{false};
+  parallel_chunks(m.numel, 16384, [&](int64_t t0, int64_t t1) {
+    for (int64_t t = t0; t < t1; t++) {
+      int el = s.elem_order[t];
+      const int32_t *c = &m.ix[(size_t)el * nen1];
+      int nv = elem_nodes(type_of(el));
+      int pair = 0;
+      for (int a = 0; a < nen; a++)
+        for (int b = a + 1; b < nen; b++, pair++) {
+          if (a >= nv || b >= nv) continue;
+          int va = c[a] - 1, vb = c[b] - 1;
+          if (!first[va] || !first[vb] || va == vb) continue;
+          int hi = first[va] > first[vb] ? va : vb;
+          int lo = hi == va ? vb : va;
+          int32_t r = first[hi] - 1;  // 0-based row of the higher node's first dof
+          const int32_t *rb = s.ja.data() + (s.ia[r] - 1);
+          const int32_t *re = s.ja.data() + (s.ia[r + 1] - 1);
+          const int32_t *pos = std::lower_bound(rb, re, first[lo]);
+          if (pos == re || *pos != first[lo]) {
+            missing = true;
+            continue;
+          }
+          s.slot[(size_t)pair * m.numel + t] = (int32_t)(pos - rb);
+        }
+    }
+  });
+  ELX_REQUIRE(!missing, ELX_ERR_ARG, "CSRC pattern does not contain an element's node pair");
 }
 
 namespace {
@@ -555,27 +612,41 @@ void build_blocks(Structure &s, int bsize) {
   if (B < 2 || B > 3 || s.neq % B) return;
   const int nb = s.neq / B;
   std::vector<int32_t> nl(nb), nup(nb, 0);
-  for (int I = 0; I < nb; I++) {
-    const int r0 = B * I;
-    const int32_t k0 = s.ia[r0] - 1;
-    const int32_t len0 = s.ia[r0 + 1] - s.ia[r0];
-    if (len0 % B) return;
-    const int n = len0 / B;
-    nl[I] = n;
-    for (int a = 0; a < B; a++) {
-      const int r = r0 + a;
-      const int32_t k = s.ia[r] - 1;
-      if (s.ia[r + 1] - s.ia[r] != B * n + a) return;
-      for (int q = 0; q < n; q++) {
-        const int c0 = s.ja[k0 + B * q] - 1;
-        if (c0 % B || c0 / B >= I) return;
-        for (int b = 0; b < B; b++)
-          if (s.ja[k + B * q + b] - 1 != c0 + b) return;
+  // every row block I: B rows of whole B x B blocks left of the diagonal
+  // block (the same block columns in each row) plus the diagonal block's
+  // lower part
+  std::atomic<bool> not_blocked{false};
+  parallel_chunks(nb, 8192, [&](int64_t I0, int64_t I1) {
+    for (int64_t I = I0; I < I1 && !not_blocked.load(std::memory_order_relaxed); I++) {
+      const int r0 = B * (int)I;
+      const int32_t k0 = s.ia[r0] - 1;
+      const int32_t len0 = s.ia[r0 + 1] - s.ia[r0];
+      bool ok = len0 % B == 0;
+      const int n = len0 / B;
+      nl[I] = n;
+      for (int a = 0; ok && a < B; a++) {
+        const int r = r0 + a;
+        const int32_t k = s.ia[r] - 1;
+        if (s.ia[r + 1] - s.ia[r] != B * n + a) {
+          ok = false;
+          break;
+        }
+        for (int q = 0; ok && q < n; q++) {
+          const int c0 = s.ja[k0 + B * q] - 1;
+          if (c0 % B || c0 / B >= I) ok = false;
+          for (int b = 0; ok && b < B; b++)
+            if (s.ja[k + B * q + b] - 1 != c0 + b) ok = false;
+        }
+        for (int t = 0; ok && t < a; t++)
+          if (s.ja[k + B * n + t] - 1 != r0 + t) ok = false;
       }
-      for (int t = 0; t < a; t++)
-        if (s.ja[k + B * n + t] - 1 != r0 + t) return;
+      if (!ok) not_blocked = true;
     }
-    for (int q = 0; q < n; q++) nup[(s.ja[k0 + B * q] - 1) / B]++;
+  });
+  if (not_blocked) return;
+  for (int I = 0; I < nb; I++) {
+    const int32_t k0 = s.ia[B * I] - 1;
+    for (int q = 0; q < nl[I]; q++) nup[(s.ja[k0 + B * q] - 1) / B]++;
   }
   s.bia.assign(nb + 1, 0);
   for (int I = 0; I < nb; I++) s.bia[I + 1] = s.bia[I] + nl[I] + 1 + nup[I];
@@ -614,15 +685,17 @@ void build_blocks(Structure &s, int bsize) {
     s.sell_ptr[sl + 1] = s.sell_ptr[sl] + w;
   }
   s.sell_col.assign((size_t)s.sell_ptr[s.nslices] * R, 0);
-  for (int sl = 0; sl < s.nslices; sl++)
-    for (int t = 0; t < R; t++) {
-      const int I = sl * R + t;
-      const int n = I < nb ? s.bia[I + 1] - s.bia[I] : 0;
-      for (int g = s.sell_ptr[sl]; g < s.sell_ptr[sl + 1]; g++) {
-        const int k = g - s.sell_ptr[sl];
-        s.sell_col[(size_t)g * R + t] = k < n ? s.bja[s.bia[I] + k] : (I < nb ? I : 0);
+  parallel_chunks(s.nslices, 1024, [&](int64_t sl0, int64_t sl1) {
+    for (int64_t sl = sl0; sl < sl1; sl++)
+      for (int t = 0; t < R; t++) {
+        const int I = (int)sl * R + t;
+        const int n = I < nb ? s.bia[I + 1] - s.bia[I] : 0;
+        for (int g = s.sell_ptr[sl]; g < s.sell_ptr[sl + 1]; g++) {
+          const int k = g - s.sell_ptr[sl];
+          s.sell_col[(size_t)g * R + t] = k < n ? s.bja[s.bia[I] + k] : (I < nb ? I : 0);
+        }
       }
-    }
+  });
 }
 
 }  // namespace elx
