@@ -113,8 +113,17 @@ struct elx_ctx {
     if (budget > 0 && used + (int64_t)bytes > budget)
       throw Error{ELX_ERR_OOM, "HBM budget exceeded: need " + std::to_string(bytes) +
                                    " more bytes, " + std::to_string(budget - used) + " left"};
-    const cudaError_t me =
+    cudaError_t me =
         pool ? cudaMallocFromPoolAsync(&d.p, bytes, pool, stream) : cudaMalloc(&d.p, bytes);
+    if (me != cudaSuccess && pool) {
+      // the pool keeps freed memory reserved: hand what none of its users
+      // holds back to the device (this stream's own frees done first) and
+      // try once more
+      (void)cudaGetLastError();
+      cudaStreamSynchronize(stream);
+      cudaMemPoolTrimTo(pool, 0);
+      me = cudaMallocFromPoolAsync(&d.p, bytes, pool, stream);
+    }
     if (me != cudaSuccess) {
       d.p = nullptr;
       (void)cudaGetLastError();
