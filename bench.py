@@ -16,7 +16,9 @@ recovery and writer; the product through 4 row-block partitions), `block`
 (16 load cases of the 96x96x48 plate), `tetra` (FP64 and mixed PCG to 1e-10
 on the 48^3 TETRA4 mesh with per-element materials, against the oracle's
 FP64 solve) and `serve` (a served request stream against sequential plain
-FP64 solves).
+FP64 solves; `served.phases_mean_s` splits the packed and the block-solved
+requests' mean latency into preparation, waiting for admission, admission,
+waiting to start and solve).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
