@@ -176,31 +176,18 @@ int pseudo_peripheral(int root, const std::vector<int32_t> &xadj,
 void rcm_order(int32_t n, const std::vector<int32_t> &xadj,
                const std::vector<int32_t> &adj, std::vector<int32_t> &perm) {
   perm.assign(n, 0);
-  std::vector<char> mask(n, 1), seen(n, 0);
-  std::vector<int32_t> xls(n + 2), deg(n, 0);
+  std::vector<char> mask(n, 1);
+  std::vector<int32_t> xls(n + 2);
+  // the masked degree the ordering sorts by (degree, Reord.f:355-435) counts
+  // a node's unnumbered neighbours; a component is numbered only once all
+  // of it is reached, so while it is being numbered every neighbour of its
+  // nodes is unnumbered and the masked degree is the node's full degree
+  auto deg = [&](int v) { return xadj[v + 1] - xadj[v]; };
   int num = 0;
   for (int i = 0; i < n && num < n; i++) {
     if (!mask[i]) continue;
     int32_t *ls = perm.data() + num;
     int root = pseudo_peripheral(i, xadj, adj, mask, ls, xls);
-    // masked degrees of the component (degree, Reord.f:355-435)
-    int size = 1;
-    ls[0] = root;
-    seen[root] = 1;
-    for (int h = 0; h < size; h++) {
-      int v = ls[h], d = 0;
-      for (int k = xadj[v]; k < xadj[v + 1]; k++) {
-        int w = adj[k];
-        if (!mask[w]) continue;
-        d++;
-        if (!seen[w]) {
-          seen[w] = 1;
-          ls[size++] = w;
-        }
-      }
-      deg[v] = d;
-    }
-    for (int h = 0; h < size; h++) seen[ls[h]] = 0;
     // Cuthill-McKee numbering (rcm, Reord.f:170-265)
     mask[root] = 0;
     ls[0] = root;
@@ -217,15 +204,16 @@ void rcm_order(int32_t n, const std::vector<int32_t> &xadj,
       // stable insertion sort of the new neighbours by degree
       for (int a = first_new + 1; a < last; a++) {
         int w = ls[a], b = a - 1;
-        while (b >= first_new && deg[ls[b]] > deg[w]) {
+        const int dw = deg(w);
+        while (b >= first_new && deg(ls[b]) > dw) {
           ls[b + 1] = ls[b];
           b--;
         }
         ls[b + 1] = w;
       }
     }
-    std::reverse(ls, ls + size);
-    num += size;
+    std::reverse(ls, ls + last);  // the component: all `last` nodes reached
+    num += last;
   }
 }
 
