@@ -53,7 +53,7 @@ def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) 
 
 
 def _build(force: bool, verbose: bool, ptxas_info: bool) -> str:
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "elastic_gb300.h"))
     nv = nvcc()
     jobs = []
